@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark of the VEGAS+ iteration loop on one GB300 (replicas on N GPUs).
+
+Workload (default): Gaussian family, d=8, width 0.1, centre 0.5, 1e8 integrand
+evaluations per iteration, 1024 bins per dimension, alpha=0.5, beta=0.75,
+seed 0, 20 iterations -- FP32 evaluation with Kahan-compensated f/f^2
+accumulation and FP64 mean/variance/grid ("chosen" form).  A step is one
+VEGAS+ iteration: fill (sample, map, integrand, accumulate), hypercube
+reallocation, grid refinement.
+
+Printed JSON line (rank 0):
+  value      evals/s over the K timed iterations, state resident in HBM
+  e2e        evals/s of whole integrations through the C ABI with host
+             parameters in and host results out (cvg_integrate)
+  plain      the same workload in the plain FP64 form
+  roofline   fill kernel: algorithmic FP32 ops per evaluation x evaluations
+             per launch / CUDA-event launch time, against a live FP32 FMA
+             microbenchmark of the same GPU
+  cpu_baseline  the CPU oracle (FP64, OpenMP, all host cores) on a bounded
+             sample of the same workload
+`--impl reference` times the reference's computation on the host cores (the
+CPU restatement of the reference loop in oracle/, FP64).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIM, N_IT, NBINS, ITERS, SEED = 8, 100_000_000, 1024, 20, 0
+FLOPS_PER_EVAL = 11 * DIM + 4          # algorithmic FP32 ops per evaluation
+METRIC = "integrand evals/s, VEGAS+ Gaussian d=8, 1e8 evals/iteration (FP32-compensated form)"
+WORKLOAD = "gauss-d8-1e8x20-fp32kahan"
+LAUNCHES_PER_IT = 7                    # fill + refine + 5 reallocation kernels
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _ncu_traffic():
+    """DRAM bytes per fill launch from the committed ncu summary (or None)."""
+    p = os.path.join(ROOT, "profiles", "fill_gauss_d8_traffic.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch_full_size="):
+                return float(line.split("=", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_oracle_rate(n_it, iters, threads=0):
+    """Oracle (FP64 restatement of the reference loop) on host cores: evals/s."""
+    import numpy as np
+    from oracle import pyoracle as P
+    r = P.OracleRun(DIM, n_it * (iters + 1), iters + 1, n_intervals=NBINS)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=SEED)
+    th = np.array([0.5, 0.1])
+    tot, t0 = 0, time.perf_counter()
+    for it in range(iters):
+        tot += r.fill(P.F_GAUSS, th, u, it=it, n_threads=threads)
+        d, _, _ = r.results()
+        r.refine()
+        r.update_nh(d)
+    dt = time.perf_counter() - t0
+    return tot / dt, tot, dt
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.destroy_process_group()
+            return
+    import numpy as np
+    from oracle import pyoracle as P
+    cores = os.cpu_count() or 1
+    n_it = 10_000_000         # bounded sample per step (same d, bins, integrand)
+    steps, warm = args.steps, args.warmup
+    r = P.OracleRun(DIM, n_it * (steps + warm + 1), steps + warm + 1, n_intervals=NBINS)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=SEED)
+    th = np.array([0.5, 0.1])
+    tot, el = 0, 0.0
+    for it in range(warm + steps):
+        t0 = time.perf_counter()
+        n = r.fill(P.F_GAUSS, th, u, it=it)
+        d, _, _ = r.results()
+        r.refine()
+        r.update_nh(d)
+        dt = time.perf_counter() - t0
+        if it >= warm:
+            tot += n
+            el += dt
+    v = tot / el
+    sample = "%d VEGAS+ iterations of the d=8 Gaussian workload at %d evals/iteration " \
+             "(1024 bins), FP64" % (steps, n_it)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "evals/s",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+            "ms_per_step": 1e3 * el / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "dim": DIM, "evals_per_iteration": n_it,
+                       "nbins": NBINS, "implementation": "CPU restatement of the reference "
+                       "VEGAS+ loop (oracle/vegas_oracle.c), OpenMP over hypercubes"},
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def timed_iterations(run, n, stream, torch):
+    """Run n iterations with a CUDA event between each; returns per-iteration ms."""
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+    evs[0].record(stream)
+    for i in range(n):
+        run.iterate(1)
+        evs[i + 1].record(stream)
+    stream.synchronize()
+    return [evs[i].elapsed_time(evs[i + 1]) for i in range(n)]
+
+
+def time_to_rel(it_res, it_sig, it_ms, skip, target=1e-4, exact=None):
+    """Time from the first iteration until the running weighted estimate
+    reaches err/|I| <= target (and |I-exact| <= 3 err when exact is known)."""
+    sw = swr = 0.0
+    t = 0.0
+    for i in range(len(it_ms)):
+        t += it_ms[i]
+        if i < skip:
+            continue
+        sw += 1.0 / it_sig[i]
+        swr += it_res[i] / it_sig[i]
+        I, err = swr / sw, 1.0 / math.sqrt(sw)
+        if err / abs(I) <= target and (exact is None or abs(I - exact) <= 3 * err):
+            return t / 1e3, i + 1, I, err
+    return None, None, None, None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from cuvegas_gb300 import _build, _lib as L, runtime, integrands as I
+    from oracle import analytic as A
+    _build.build()
+    stream = torch.cuda.Stream(device=local)
+    ctx = runtime.Context(local, stream=C_stream(stream))
+    f = ctx.integrand(I.GAUSS, DIM)
+    exact = A.gauss_normalised(DIM)
+    steps, warm = args.steps, args.warmup
+    skip = 5
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def measure(prec, n_it):
+        p = runtime.make_params(DIM, n_it * (warm + steps), warm + steps, skip=min(skip, warm + steps - 1),
+                                n_intervals=NBINS, seed=SEED + rank, precision=prec,
+                                flags=L.FLAG_TIME_FILL, instance=rank)
+        with runtime.Run(f, p) as r:
+            r.iterate(warm)
+            r.sync()
+            r.fill_times()
+            barrier()
+            with ClockSampler(local) as clk:
+                t0 = time.perf_counter()
+                it_ms = timed_iterations(r, steps, stream, torch)
+                wall = time.perf_counter() - t0
+            fills = r.fill_times()
+            st = r.get(L.BUF_STATS)
+            info = r.info
+        evals = float(st[2, warm:warm + steps].sum())
+        ms = float(sum(it_ms))
+        return dict(evals=evals, ms=ms, wall=wall, fills=fills, clk=clk.summary(), info=info,
+                    samples=st[2, warm:warm + steps])
+
+    def convergence(prec, n_it, iters=ITERS):
+        p = runtime.make_params(DIM, n_it * iters, iters, skip=skip, n_intervals=NBINS,
+                                seed=SEED + rank, precision=prec, instance=rank)
+        with runtime.Run(f, p) as r:
+            it_ms = timed_iterations(r, iters, stream, torch)
+            res, it_res, it_sig = r.result()
+        t, nit, Ival, err = time_to_rel(it_res, it_sig, it_ms, skip, exact=exact)
+        return dict(time_to_1e4_s=t, iterations=nit, result=res.result, error=res.error,
+                    chi2_dof=res.chi2_dof, exact=exact, pull=(res.result - exact) / res.error,
+                    total_s=sum(it_ms) / 1e3)
+
+    # warm the JIT cache for both forms
+    for prec in (L.PREC_FP32, L.PREC_FP64):
+        with runtime.Run(f, runtime.make_params(DIM, 4 * 100000, 4, n_intervals=NBINS,
+                                                precision=prec)) as r:
+            r.iterate(4)
+            r.sync()
+
+    chosen = measure(L.PREC_FP32, N_IT)
+    # max over ranks of the timed region
+    ms_all = chosen["ms"]
+    ev_all = chosen["evals"]
+    if world > 1:
+        t = torch.tensor([ms_all, ev_all], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        ms_all, ev_all = float(mx[0]), float(t[1])
+    value = ev_all / (ms_all / 1e3)
+
+    extra = {}
+    if rank == 0 and not args.quick:
+        plain = measure(L.PREC_FP64, N_IT)
+        extra["plain"] = {"value": plain["evals"] / (plain["ms"] / 1e3), "unit": "evals/s",
+                          "ms_per_step": plain["ms"] / steps, "dtype": "f64",
+                          "fill_ms_mean": float(np.mean(plain["fills"])) if len(plain["fills"]) else None}
+        conv32 = convergence(L.PREC_FP32, N_IT)
+        conv64 = convergence(L.PREC_FP64, N_IT)
+        extra["time_to_1e-4"] = {"chosen_s": conv32["time_to_1e4_s"], "plain_s": conv64["time_to_1e4_s"],
+                                 "chosen": conv32, "plain": conv64}
+        extra["speedup_chosen_vs_plain"] = {
+            "evals_per_s": value / extra["plain"]["value"],
+            "time_to_1e-4": (conv64["time_to_1e4_s"] / conv32["time_to_1e4_s"]
+                             if conv32["time_to_1e4_s"] and conv64["time_to_1e4_s"] else None)}
+
+    # roofline of the fill kernel (chosen form)
+    fills = chosen["fills"]
+    roof = None
+    if rank == 0 and len(fills):
+        mean_ms = float(np.mean(fills))
+        evals_per_launch = float(np.mean(chosen["samples"]))
+        achieved = evals_per_launch * FLOPS_PER_EVAL / (mean_ms * 1e-3) / 1e12
+        peak = ctx.measure_peak(0)
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": _ncu_traffic(),
+                "kernel": "cvg_fill_entry (FP32, d=8, 1024 bins)",
+                "fill_ms_mean": mean_ms, "evals_per_launch": evals_per_launch,
+                "flops_per_eval": FLOPS_PER_EVAL,
+                "peak_source": "FP32 FMA microbenchmark of this GPU (cvg_measure_peak), "
+                               "live; MEASURED_PEAKS.json holds no FP32 figure",
+                "fill_share_of_step": mean_ms / (chosen["ms"] / steps)}
+
+    # end to end through the C ABI: host params in, host result out
+    e2e = None
+    if rank == 0 and not args.quick:
+        p = runtime.make_params(DIM, N_IT * ITERS, ITERS, skip=skip, n_intervals=NBINS,
+                                seed=SEED, precision=L.PREC_FP32, flags=L.FLAG_GRAPH)
+        runtime.integrate_once(f, p)              # allocator / JIT warm
+        t0 = time.perf_counter()
+        res, _, _ = runtime.integrate_once(f, p)
+        dt = time.perf_counter() - t0
+        h2d = 8 * DIM * (NBINS + 1)                # initial grid
+        d2h = 8 * 3 * ITERS + 64 + 4               # per-iteration stats, sums, status
+        e2e = {"value": res.tot_nevals / dt, "unit": "evals/s",
+               "h2d_bytes_per_step": h2d / ITERS, "d2h_bytes_per_step": d2h / ITERS,
+               "call": "cvg_integrate", "wall_s": dt, "result": res.result, "error": res.error}
+
+    cpu = None
+    if rank == 0 and not args.quick and not args.no_cpu:
+        n_cpu = 2_000_000
+        rate, tot, dt = cpu_oracle_rate(n_cpu, 3)
+        cpu = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "3 VEGAS+ iterations of the same d=8 Gaussian workload at %d "
+                         "evals/iteration, FP64 CPU oracle, %d evals in %.1f s" % (n_cpu, tot, dt)}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+                "steps": steps, "warmup": warm, "ms_per_step": ms_all / steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "dim": DIM, "evals_per_iteration": N_IT,
+                           "nbins": NBINS, "alpha": 0.5, "beta": 0.75, "seed": SEED,
+                           "n_strat": chosen["info"].n_strat, "n_cubes": chosen["info"].n_cubes,
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "l2": "per-hypercube state %.0f MB > L2 (129 MB), streamed every "
+                                 "iteration" % (chosen["info"].n_cubes * 36 / 1e6)},
+                "gpu_launches": LAUNCHES_PER_IT * steps,
+                "clocks": chosen["clk"], "roofline": roof, "cpu_baseline": cpu, "e2e": e2e}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def C_stream(stream):
+    import ctypes
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=17)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="headline number only")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,111 @@
+// cvg_common.cuh -- types and device helpers shared by the NVRTC-compiled
+// fill kernels, the precompiled reallocation/refinement kernels and the host
+// driver.  Self-contained (no includes) so NVRTC can compile it as-is.
+#ifndef CVG_COMMON_CUH
+#define CVG_COMMON_CUH
+
+typedef unsigned int cvg_u32;
+typedef unsigned long long cvg_u64;
+typedef long long cvg_i64;
+
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+#define CVG_HD __host__ __device__ __forceinline__
+#define CVG_D __device__ __forceinline__
+#else
+#define CVG_HD inline
+#endif
+
+// Status bits written by kernels into the run's status word.
+#define CVG_KSTAT_BAD_TILE 1u      // tile map inconsistent with nh_sum
+#define CVG_KSTAT_NONFINITE 2u     // a non-finite per-cube estimate was seen
+
+// Arguments of one fill launch.  Layout is shared between host and device;
+// only fixed-width scalar types and pointers.
+struct cvg_fill_args {
+    const double *x_edges;        // [dim][N+1] FP64 grid
+    const float *x_edges32;       // [dim][N+1] FP32 copy of the grid
+    const cvg_u64 *nh_sum;        // [n_cubes+1] exclusive prefix of samples per cube
+    const cvg_u32 *tile_cube;     // [max_tiles] cube holding the first sample of each tile
+    const cvg_u32 *iteration;     // device iteration counter (Philox counter word 2)
+    const float *ubuf;            // replay uniforms [S][dim] (test path), else null
+    const double *theta;          // integrand parameters [n_params], or null
+    double *JF;                   // [n_cubes] sum of f*jac per cube
+    double *JF2;                  // [n_cubes] sum of (f*jac)^2 per cube
+    double *weights;              // [dim][N] sum of (f*jac)^2 per bin
+    cvg_u32 *counts;              // [dim][N] samples per bin
+    double *grad;                 // [n_params] dI/dtheta accumulator (gradient pass)
+    cvg_u32 *status;              // error bits
+    cvg_u64 max_tiles;            // capacity of tile_cube
+    cvg_u64 seed;                 // Philox key
+    cvg_u32 instance;             // Philox counter word 3, bits 8..31
+    cvg_u32 n_cubes;
+    int n_strat;
+    int n_intervals;
+    int tile_samples;             // samples per tile = blockDim.x * spt
+    int spt;                      // consecutive samples per thread
+    int n_params;
+    int pad0;
+    double v_cubes;               // volume of one hypercube
+};
+
+CVG_HD cvg_u64 cvg_align16(cvg_u64 x) { return (x + 15ull) & ~15ull; }
+
+// Dynamic shared memory of one fill launch; the kernel carves it in the same
+// order: theta | bin sums | grid | bin counts | cube starts | reduce scratch.
+CVG_HD cvg_u64 cvg_fill_smem_bytes(int dim, int n_intervals, int tsz, int edges_smem,
+                                   int hist_smem, int grad, int tile_samples, int n_params,
+                                   int block)
+{
+    cvg_u64 b = cvg_align16((cvg_u64)n_params * tsz);
+    const int h = hist_smem && !grad;
+    if (h) b += cvg_align16((cvg_u64)dim * n_intervals * tsz);
+    if (edges_smem) b += cvg_align16((cvg_u64)dim * (n_intervals + 1) * tsz);
+    if (h) b += cvg_align16((cvg_u64)dim * n_intervals * 4);
+    b += cvg_align16((cvg_u64)(tile_samples / 2 + 4) * 4);
+    if (grad) b += cvg_align16((cvg_u64)(block / 32) * n_params * 8);
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64-bit
+// multiplies with multipliers 0xD2511F53 / 0xCD9E8D57 and a Weyl key schedule
+// (0x9E3779B9, 0xBB67AE85).  Counter = (sample-in-cube, cube, iteration,
+// dim-block | instance << 8); key = seed.
+// ---------------------------------------------------------------------------
+#if defined(__CUDACC__) || defined(__CUDACC_RTC__)
+struct cvg_u32x4 { cvg_u32 x, y, z, w; };
+
+CVG_D cvg_u32x4 cvg_philox(cvg_u32 c0, cvg_u32 c1, cvg_u32 c2, cvg_u32 c3, cvg_u32 k0,
+                           cvg_u32 k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const cvg_u32 lo0 = 0xD2511F53u * c0;
+        const cvg_u32 hi0 = __umulhi(0xD2511F53u, c0);
+        const cvg_u32 lo1 = 0xCD9E8D57u * c2;
+        const cvg_u32 hi1 = __umulhi(0xCD9E8D57u, c2);
+        const cvg_u32 n0 = hi1 ^ c1 ^ k0;
+        const cvg_u32 n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    cvg_u32x4 o; o.x = c0; o.y = c1; o.z = c2; o.w = c3;
+    return o;
+}
+
+// 32 random bits -> uniform in (0,1).
+//  float : (2*(r>>9)+1) * 2^-24, built by exponent splicing (no int->float convert)
+//  double: (r + 0.5) * 2^-32, built the same way; both exact.
+template <typename T> CVG_D T cvg_uniform(cvg_u32 r);
+template <> CVG_D float cvg_uniform<float>(cvg_u32 r)
+{
+    return __uint_as_float(0x3F800000u | (r >> 9)) - 0.99999994039535522461f;
+}
+template <> CVG_D double cvg_uniform<double>(cvg_u32 r)
+{
+    return __hiloint2double((int)(0x3FF00000u | (r >> 12)), (int)(r << 20)) -
+           0.99999999988358467817;  // 1 - 2^-33
+}
+#endif  // device
+
+#endif  // CVG_COMMON_CUH

@@ -1,0 +1,276 @@
+// cvg_fill.cuh -- the fused VEGAS+ fill: counter-based sampling, map through
+// the adaptive grid, integrand, per-hypercube and per-bin accumulation.
+//
+// Replaces vegasFill of the reference (src/main.cu:20-79 and
+// vegas_cuda/src/vegas_cuda_extension/cuda_kernel.cu:14-76) together with the
+// evals[] expansion it depends on (mapCubes, src/main.cu:248-262), the curand
+// state it carries (setup_kernel, src/main.cu:12-18) and the accumulator
+// resets (src/main.cu:147-171).
+//
+// Work decomposition.  Samples of one iteration are numbered s = 0..S-1 in
+// cube order (cube c owns [nh_sum[c], nh_sum[c+1])), exactly the order of the
+// reference's evals[] array.  A persistent grid walks fixed-size tiles of
+// tile_samples consecutive samples; thread t of a tile owns spt consecutive
+// samples, so a thread stays inside one cube for a run of samples and keeps
+// Sum f*jac and Sum (f*jac)^2 of that run in registers (compensated in FP32).
+// A run ends at a cube boundary or at the end of the thread's slice and is
+// added to JF/JF2 with one FP64 atomic each.  Per-bin Sum (f*jac)^2 and counts
+// go to shared-memory histograms, added to the global FP64/u32 histograms
+// once per CTA at the end.
+//
+// Expects, before inclusion: cvg_common.cuh, and the macros
+//   CVG_F(x, th)          -> integrand value at x (T* x, const T* th)
+//   CVG_DF(x, th, g)      -> gradient w.r.t. theta into g[] (gradient pass only)
+#ifndef CVG_FILL_CUH
+#define CVG_FILL_CUH
+
+template <typename T> struct cvg_grid_src;
+template <> struct cvg_grid_src<float> {
+    static CVG_D const float *get(const cvg_fill_args &a) { return a.x_edges32; }
+};
+template <> struct cvg_grid_src<double> {
+    static CVG_D const double *get(const cvg_fill_args &a) { return a.x_edges; }
+};
+
+// Running sum of one cube run.  FP32: Kahan-compensated; FP64: plain.
+template <typename T> struct cvg_acc;
+template <> struct cvg_acc<float> {
+    float s, k;
+    CVG_D void reset() { s = 0.f; k = 0.f; }
+    CVG_D void add(float x) { const float y = x - k; const float t = s + y; k = (t - s) - y; s = t; }
+    CVG_D double value() const { return (double)s - (double)k; }
+};
+template <> struct cvg_acc<double> {
+    double s;
+    CVG_D void reset() { s = 0.0; }
+    CVG_D void add(double x) { s += x; }
+    CVG_D double value() const { return s; }
+};
+
+CVG_D float cvg_fma(float a, float b, float c) { return fmaf(a, b, c); }
+CVG_D double cvg_fma(double a, double b, double c) { return fma(a, b, c); }
+
+// Stratum offsets coord_d * dy of cube c (digit d of c in base n_strat, least
+// significant first: src/main.cu:43-47).
+template <int D, typename T>
+CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, T *cdy)
+{
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const cvg_u32 q = c / ns;
+        cdy[d] = (T)(c - q * ns) * dy;
+        c = q;
+    }
+}
+
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD>
+CVG_D void cvg_fill_body(const cvg_fill_args &a)
+{
+    extern __shared__ __align__(16) unsigned char cvg_smem[];
+    constexpr int PP = P > 0 ? P : 1;
+    constexpr int NB = (D + 3) / 4;
+    const int N = a.n_intervals;
+    const int tid = threadIdx.x;
+    const cvg_u64 S = a.nh_sum[a.n_cubes];
+    const int TS = a.tile_samples;
+    cvg_u64 n_tiles = (S + (cvg_u64)TS - 1) / (cvg_u64)TS;
+    if (n_tiles > a.max_tiles) {   // never produced by the reallocation; keep accesses in bounds
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
+        n_tiles = a.max_tiles;
+    }
+    if ((cvg_u64)blockIdx.x >= n_tiles) return;
+
+    // ---- shared memory carve (same order as cvg_fill_smem_bytes) ----
+    constexpr bool H = HSM && !GRAD;
+    cvg_u64 off = 0;
+    T *th = (T *)(cvg_smem + off);
+    off += cvg_align16((cvg_u64)P * sizeof(T));
+    T *hw = (T *)(cvg_smem + off);
+    if (H) off += cvg_align16((cvg_u64)D * N * sizeof(T));
+    T *E = (T *)(cvg_smem + off);
+    if (ESM) off += cvg_align16((cvg_u64)D * (N + 1) * sizeof(T));
+    cvg_u32 *hc = (cvg_u32 *)(cvg_smem + off);
+    if (H) off += cvg_align16((cvg_u64)D * N * 4);
+    int *starts = (int *)(cvg_smem + off);
+    off += cvg_align16((cvg_u64)(TS / 2 + 4) * 4);
+    double *red = (double *)(cvg_smem + off);
+
+    const T *grid = cvg_grid_src<T>::get(a);
+    if (P > 0)
+        for (int i = tid; i < P; i += BS) th[i] = (T)a.theta[i];
+    if (ESM)
+        for (int i = tid; i < D * (N + 1); i += BS) E[i] = grid[i];
+    if (H)
+        for (int i = tid; i < D * N; i += BS) { hw[i] = (T)0; hc[i] = 0u; }
+
+    const cvg_u32 it = *a.iteration;
+    const cvg_u32 k0 = (cvg_u32)a.seed, k1 = (cvg_u32)(a.seed >> 32);
+    const cvg_u32 c3 = a.instance << 8;
+    const cvg_u32 ns = (cvg_u32)a.n_strat;
+    const T dy = (T)1 / (T)a.n_strat;
+    const T fN = (T)N;
+    const T *G = ESM ? E : grid;
+
+    double gtot[PP];
+#pragma unroll
+    for (int p = 0; p < PP; ++p) gtot[p] = 0.0;
+
+    __syncthreads();
+
+    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const cvg_u64 base = tile * (cvg_u64)TS;
+        const cvg_u32 c_lo = a.tile_cube[tile];
+        const cvg_u32 c_hi = (tile + 1 < n_tiles) ? a.tile_cube[tile + 1] : a.n_cubes - 1;
+        if (c_hi < c_lo || c_hi >= a.n_cubes || (int)(c_hi - c_lo) > TS / 2 + 1) {
+            if (tid == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
+            break;  // uniform across the block
+        }
+        const int K = (int)(c_hi - c_lo) + 2;
+        for (int i = tid; i < K; i += BS)
+            starts[i] = (int)((cvg_i64)a.nh_sum[c_lo + i] - (cvg_i64)base);
+        __syncthreads();
+
+        const int spt = a.spt;
+        const int l0 = tid * spt;
+        const cvg_u64 rem = S - base;
+        const int lend_tile = rem < (cvg_u64)TS ? (int)rem : TS;
+        if (l0 < lend_tile) {
+            int lo = 0, hi = K - 2;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (starts[mid] <= l0) lo = mid; else hi = mid - 1;
+            }
+            int ci = lo;
+            cvg_u32 c = c_lo + (cvg_u32)ci;
+            int next = starts[ci + 1];
+            cvg_u32 j = (cvg_u32)(l0 - starts[ci]);
+            T cdy[D];
+            cvg_cube_offsets<D, T>(c, ns, dy, cdy);
+            const int lend = min(l0 + spt, lend_tile);
+
+            cvg_acc<T> a1, a2;
+            a1.reset(); a2.reset();
+            T ag[PP];
+#pragma unroll
+            for (int p = 0; p < PP; ++p) ag[p] = (T)0;
+            int run = 0;  // samples in the current cube run
+
+            for (int l = l0; l < lend; ++l) {
+                if (l >= next) {
+                    if (run > 0) {
+                        if (GRAD) {
+                            const double sc = a.v_cubes / (double)(next - starts[ci]);
+#pragma unroll
+                            for (int p = 0; p < PP; ++p) { gtot[p] += (double)ag[p] * sc; ag[p] = (T)0; }
+                        } else {
+                            atomicAdd(&a.JF[c], a1.value());
+                            atomicAdd(&a.JF2[c], a2.value());
+                            a1.reset(); a2.reset();
+                        }
+                        run = 0;
+                    }
+                    do {  // empty cubes (never produced by the reallocation) are skipped
+                        ++ci; ++c;
+                        next = starts[ci + 1];
+                    } while (l >= next && ci < K - 2);
+                    j = 0u;
+                    cvg_cube_offsets<D, T>(c, ns, dy, cdy);
+                }
+                ++run;
+                cvg_u32 rr[NB * 4];
+                if (!REPLAY) {
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) {
+                        const cvg_u32x4 r4 = cvg_philox(j, c, it, (cvg_u32)b | c3, k0, k1);
+                        rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y;
+                        rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
+                    }
+                }
+                T x[D];
+                int bin[D];
+                T jac = (T)1;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    T u;
+                    if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
+                    else u = cvg_uniform<T>(rr[d]);
+                    const T y = cvg_fma(u, dy, cdy[d]);
+                    const T z = y * fN;
+                    int b = (int)z;
+                    b = b < N - 1 ? b : N - 1;
+                    b = b > 0 ? b : 0;
+                    const T e0 = G[d * (N + 1) + b];
+                    const T e1 = G[d * (N + 1) + b + 1];
+                    const T dx = e1 - e0;
+                    x[d] = cvg_fma(dx, z - (T)b, e0);
+                    jac *= fN * dx;
+                    bin[d] = b;
+                }
+                if (GRAD) {
+#if defined(CVG_HAS_GRAD)
+                    T g[PP];
+                    CVG_DF(x, th, g);
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) ag[p] += g[p] * jac;
+#endif
+                } else {
+                    const T jf = (T)CVG_F(x, th) * jac;
+                    const T jf2 = jf * jf;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        if (H) {
+                            atomicAdd(&hw[d * N + bin[d]], jf2);
+                            atomicAdd(&hc[d * N + bin[d]], 1u);
+                        } else {
+                            atomicAdd(&a.weights[d * N + bin[d]], (double)jf2);
+                            atomicAdd(&a.counts[d * N + bin[d]], 1u);
+                        }
+                    }
+                    a1.add(jf);
+                    a2.add(jf2);
+                }
+                ++j;
+            }
+            if (run > 0) {
+                if (GRAD) {
+                    const double sc = a.v_cubes / (double)(starts[ci + 1] - starts[ci]);
+#pragma unroll
+                    for (int p = 0; p < PP; ++p) gtot[p] += (double)ag[p] * sc;
+                } else {
+                    atomicAdd(&a.JF[c], a1.value());
+                    atomicAdd(&a.JF2[c], a2.value());
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    if (H) {
+        __syncthreads();
+        for (int i = tid; i < D * N; i += BS) {
+            const cvg_u32 cn = hc[i];
+            if (cn) {
+                atomicAdd(&a.weights[i], (double)hw[i]);
+                atomicAdd(&a.counts[i], cn);
+            }
+        }
+    }
+    if (GRAD) {
+        const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+            double v = gtot[p];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp * PP + p] = v;
+        }
+        __syncthreads();
+        if (tid < PP && tid < P) {
+            double v = 0.0;
+            for (int w = 0; w < BS / 32; ++w) v += red[w * PP + tid];
+            atomicAdd(&a.grad[tid], v);
+        }
+    }
+}
+
+#endif  // CVG_FILL_CUH

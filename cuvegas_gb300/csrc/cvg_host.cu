@@ -1,0 +1,1032 @@
+// cvg_host.cu -- host driver and C ABI of libcuvegas.
+//
+// Replaces the host side of the reference: the per-call setup, allocation and
+// iteration loop of integrate_cuda / main (cuda_wrapper.cu:290-872,
+// src/main.cu:277-800) and the JIT link step (cuda_wrapper.cu:221-286).
+//
+// GB300-first choices:
+//  * one context per device, caller's stream or its own; no host sync inside
+//    an iteration -- the sample count, iteration counter, weighted-mean sums
+//    and chi^2 inputs live on the device until the caller asks for them;
+//  * integrand source -> NVRTC -> sm_103a cubin, with the fill kernel
+//    specialised on dimension, precision and tile shape and the integrand
+//    inlined; cubins cached in memory and on disk;
+//  * an iteration can be captured once as a CUDA graph and replayed.
+#include "cuvegas.h"
+#include "cvg_kernels.cuh"
+
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <unordered_map>
+#include <vector>
+
+#include "cvg_embedded.inc"   // cvg_src_common, cvg_src_fill (generated at build time)
+
+#define CVG_VERSION "cuvegas_gb300 0.1"
+
+namespace {
+
+thread_local std::string g_err;
+
+cvg_status fail(cvg_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+#define CK(x)                                                                          \
+    do {                                                                               \
+        cudaError_t e_ = (x);                                                          \
+        if (e_ != cudaSuccess)                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? CVG_ERR_NOMEM : CVG_ERR_CUDA, \
+                        std::string(#x) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+#define CKS(x)                                   \
+    do {                                         \
+        cvg_status s_ = (x);                     \
+        if (s_ != CVG_OK) return s_;             \
+    } while (0)
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+uint64_t fnv1a(const std::string &s, uint64_t h = 1469598103934665603ull)
+{
+    for (unsigned char c : s) { h ^= c; h *= 1099511628211ull; }
+    return h;
+}
+
+}  // namespace
+
+struct cvg_context_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int n_sm = 0;
+    int smem_optin = 0;
+    int cc_major = 0, cc_minor = 0;
+    std::string arch;
+    std::mutex mu;
+    std::unordered_map<uint64_t, cudaLibrary_t> libs;
+};
+
+struct cvg_integrand_s {
+    cvg_context ctx = nullptr;
+    std::string source;
+    int dim = 0, abi = 0, n_params = 0, has_grad = 0;
+};
+
+struct fill_variant {
+    cudaKernel_t kernel = nullptr;
+    size_t smem = 0;
+    int occ = 0;
+};
+
+struct cvg_run_s {
+    cvg_context ctx = nullptr;
+    cvg_integrand f = nullptr;
+    cvg_params p{};
+    // sizes
+    int64_t n_eval_it = 0;
+    int n_strat = 0;
+    cvg_u32 n_cubes = 0;
+    double v_cubes = 0.0;
+    unsigned nb = 0;
+    cvg_u64 max_tiles = 0;
+    int block = 0, spt = 0, TS = 0, grid = 0, esm = 1, hsm = 1;
+    int it_done = 0;
+    // device memory (one arena)
+    void *arena = nullptr;
+    double *x_edges = nullptr, *weights = nullptr, *JF = nullptr, *JF2 = nullptr, *dh = nullptr;
+    double *partials = nullptr, *stats = nullptr, *theta = nullptr, *grad = nullptr;
+    float *x_edges32 = nullptr, *ubuf = nullptr;
+    cvg_u32 *counts = nullptr, *nh_new = nullptr, *tile_cube = nullptr, *iteration = nullptr;
+    cvg_u32 *status = nullptr;
+    cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
+    cvg_acc_dev *acc = nullptr;
+    size_t ubuf_samples = 0;
+    bool replay = false;
+    fill_variant fill, fill_replay, gradk;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fill_ev;   // timed fills
+    size_t fill_ev_used = 0;
+    cudaEvent_t ev0_own = nullptr, ev1_own = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// JIT
+// ---------------------------------------------------------------------------
+namespace {
+
+std::string cache_dir()
+{
+    const char *e = std::getenv("CVG_CACHE_DIR");
+    if (e && *e) return e;
+    const char *h = std::getenv("HOME");
+    return std::string(h && *h ? h : "/tmp") + "/.cache/cuvegas_gb300";
+}
+
+void mkdirs(const std::string &path)
+{
+    std::string cur;
+    for (size_t i = 0; i < path.size(); ++i) {
+        cur.push_back(path[i]);
+        if (path[i] == '/' || i + 1 == path.size()) mkdir(cur.c_str(), 0755);
+    }
+}
+
+bool read_file(const std::string &p, std::vector<char> &out)
+{
+    FILE *fp = std::fopen(p.c_str(), "rb");
+    if (!fp) return false;
+    std::fseek(fp, 0, SEEK_END);
+    long n = std::ftell(fp);
+    std::fseek(fp, 0, SEEK_SET);
+    out.resize(n > 0 ? (size_t)n : 0);
+    bool ok = n > 0 && std::fread(out.data(), 1, out.size(), fp) == out.size();
+    std::fclose(fp);
+    return ok;
+}
+
+void write_file(const std::string &p, const std::vector<char> &data)
+{
+    std::string tmp = p + ".tmp" + std::to_string((long)getpid());
+    FILE *fp = std::fopen(tmp.c_str(), "wb");
+    if (!fp) return;
+    bool ok = std::fwrite(data.data(), 1, data.size(), fp) == data.size();
+    std::fclose(fp);
+    if (ok) std::rename(tmp.c_str(), p.c_str());
+    else std::remove(tmp.c_str());
+}
+
+struct variant_key {
+    int dim, prec, block, esm, hsm, replay, n_params, grad, abi;
+};
+
+std::string make_source(const cvg_integrand_s &f, const variant_key &k)
+{
+    const char *T = k.prec == CVG_PREC_FP32 ? "float" : "double";
+    std::string s;
+    s += "#define CVG_JIT 1\n";
+    s += cvg_src_common;
+    s += "\nstatic constexpr int cvg_n_dim = " + std::to_string(k.dim) + ";\n";
+    s += "#line 1 \"integrand.cu\"\n";
+    s += f.source;
+    s += "\n#line 1 \"cvg_adaptor\"\n";
+    if (k.abi == CVG_ABI_NUMBA) {
+        s += "__device__ __forceinline__ double cvg_numba_call(double* x) { double r = 0.0; "
+             "integrand(&r, x); return r; }\n";
+        s += "#define CVG_F(x, th) cvg_numba_call(x)\n";
+    } else if (k.n_params > 0) {
+        s += "#define CVG_F(x, th) integrand(x, th)\n";
+    } else {
+        s += "#define CVG_F(x, th) integrand(x)\n";
+    }
+    if (k.grad) {
+        s += "#define CVG_HAS_GRAD 1\n#define CVG_DF(x, th, g) integrand_grad(x, th, g)\n";
+    }
+    s += cvg_src_fill;
+    char entry[512];
+    std::snprintf(entry, sizeof(entry),
+                  "\nextern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_entry("
+                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s>(a); }\n",
+                  k.block, k.dim, T, k.block, k.esm ? "true" : "false",
+                  k.hsm ? "true" : "false", k.replay ? "true" : "false", k.n_params,
+                  k.grad ? "true" : "false");
+    s += entry;
+    return s;
+}
+
+cvg_status nvrtc_cubin(const std::string &src, const std::vector<std::string> &opts,
+                       std::vector<char> &cubin, std::string &log)
+{
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "cvg_fill.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        return fail(CVG_ERR_COMPILE, "nvrtcCreateProgram failed");
+    std::vector<const char *> copts;
+    for (auto &o : opts) copts.push_back(o.c_str());
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)copts.size(), copts.data());
+    size_t logn = 0;
+    nvrtcGetProgramLogSize(prog, &logn);
+    log.assign(logn, '\0');
+    if (logn) nvrtcGetProgramLog(prog, &log[0]);
+    if (rc != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return fail(CVG_ERR_COMPILE,
+                    std::string("integrand compile failed: ") + nvrtcGetErrorString(rc) + "\n" + log);
+    }
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    cubin.resize(n);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    return CVG_OK;
+}
+
+std::vector<std::string> nvrtc_options(const std::string &arch)
+{
+    std::vector<std::string> o = {"--gpu-architecture=" + arch, "-std=c++17", "-default-device",
+                                  "-lineinfo"};
+    const char *extra = std::getenv("CVG_NVRTC_EXTRA");   // e.g. --ptxas-options=-v
+    if (extra && *extra) o.push_back(extra);
+    return o;
+}
+
+cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_key &k,
+                      cudaKernel_t *out)
+{
+    const std::string src = make_source(f, k);
+    const std::vector<std::string> opts = nvrtc_options(ctx->arch);
+    int nv_major = 0, nv_minor = 0;
+    nvrtcVersion(&nv_major, &nv_minor);
+    std::string keystr = src;
+    for (auto &o : opts) keystr += "\n" + o;
+    keystr += "\nnvrtc " + std::to_string(nv_major) + "." + std::to_string(nv_minor);
+    keystr += "\n" CVG_VERSION;
+    const uint64_t key = fnv1a(keystr);
+
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    auto it = ctx->libs.find(key);
+    cudaLibrary_t lib = nullptr;
+    if (it != ctx->libs.end()) {
+        lib = it->second;
+    } else {
+        char name[64];
+        std::snprintf(name, sizeof(name), "%016llx.cubin", (unsigned long long)key);
+        const std::string dir = cache_dir();
+        const std::string path = dir + "/" + name;
+        std::vector<char> cubin;
+        if (!read_file(path, cubin)) {
+            std::string log;
+            CKS(nvrtc_cubin(src, opts, cubin, log));
+            mkdirs(dir);
+            write_file(path, cubin);
+        }
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
+        ctx->libs[key] = lib;
+    }
+    CK(cudaLibraryGetKernel(out, lib, "cvg_fill_entry"));
+    return CVG_OK;
+}
+
+cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v)
+{
+    cvg_context ctx = r->ctx;
+    const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
+    variant_key k{r->f->dim, r->p.precision, r->block, r->esm, r->hsm, replay ? 1 : 0,
+                  r->f->n_params, grad ? 1 : 0, r->f->abi};
+    if (grad) k.hsm = 0;
+    const cvg_u64 smem = cvg_fill_smem_bytes(k.dim, r->p.n_intervals, tsz, k.esm, k.hsm, k.grad,
+                                             r->TS, k.n_params, k.block);
+    CKS(jit_kernel(ctx, *r->f, k, &v->kernel));
+    const void *fn = (const void *)v->kernel;
+    CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, r->block, smem));
+    if (occ < 1) return fail(CVG_ERR_INVALID, "fill kernel cannot be resident (smem/regs)");
+    v->smem = smem;
+    v->occ = occ;
+    return CVG_OK;
+}
+
+// Choose whether the grid and the bin histograms live in shared memory.
+void choose_layout(cvg_run_s *r)
+{
+    const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
+    const int budget = r->ctx->smem_optin;
+    const int D = r->f->dim, N = r->p.n_intervals, P = r->f->n_params;
+    const int opts[4][2] = {{1, 1}, {0, 1}, {1, 0}, {0, 0}};
+    for (auto &o : opts) {
+        if (cvg_fill_smem_bytes(D, N, tsz, o[0], o[1], 0, r->TS, P, r->block) <= (cvg_u64)budget) {
+            r->esm = o[0];
+            r->hsm = o[1];
+            return;
+        }
+    }
+    r->esm = 0;
+    r->hsm = 0;
+}
+
+cvg_realloc_args realloc_args(cvg_run_s *r)
+{
+    cvg_realloc_args a{};
+    a.nh_sum = r->nh_sum;
+    a.JF = r->JF;
+    a.JF2 = r->JF2;
+    a.dh = r->dh;
+    a.nh_new = r->nh_new;
+    a.partials = r->partials;
+    a.bsums = r->bsums;
+    a.tile_cube = r->tile_cube;
+    a.stats = r->stats;
+    a.acc = r->acc;
+    a.iteration = r->iteration;
+    a.status = r->status;
+    a.max_tiles = r->max_tiles;
+    a.n_eval_it = r->n_eval_it;
+    a.v_cubes = r->v_cubes;
+    a.beta = r->p.beta;
+    a.n_cubes = r->n_cubes;
+    a.tile_samples = r->TS;
+    a.skip = r->p.skip;
+    a.max_it = r->p.max_it;
+    a.fast_pow = r->p.precision == CVG_PREC_FP32 ? 1 : 0;
+    a.adapt = (r->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
+    return a;
+}
+
+cvg_refine_args refine_args(cvg_run_s *r)
+{
+    cvg_refine_args a{};
+    a.x_edges = r->x_edges;
+    a.x_edges32 = r->x_edges32;
+    a.weights = r->weights;
+    a.counts = r->counts;
+    a.alpha = r->p.alpha;
+    a.dim = r->f->dim;
+    a.n_intervals = r->p.n_intervals;
+    a.adapt = (r->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
+    return a;
+}
+
+cvg_fill_args fill_args(cvg_run_s *r)
+{
+    cvg_fill_args a{};
+    a.x_edges = r->x_edges;
+    a.x_edges32 = r->x_edges32;
+    a.nh_sum = r->nh_sum;
+    a.tile_cube = r->tile_cube;
+    a.iteration = r->iteration;
+    a.ubuf = r->ubuf;
+    a.theta = r->theta;
+    a.JF = r->JF;
+    a.JF2 = r->JF2;
+    a.weights = r->weights;
+    a.counts = r->counts;
+    a.grad = r->grad;
+    a.status = r->status;
+    a.max_tiles = r->max_tiles;
+    a.seed = r->p.seed;
+    a.instance = r->p.instance;
+    a.n_cubes = r->n_cubes;
+    a.n_strat = r->n_strat;
+    a.n_intervals = r->p.n_intervals;
+    a.tile_samples = r->TS;
+    a.spt = r->spt;
+    a.n_params = r->f->n_params;
+    a.v_cubes = r->v_cubes;
+    return a;
+}
+
+cvg_status launch_fill(cvg_run_s *r, const fill_variant &v, bool timed)
+{
+    cvg_fill_args a = fill_args(r);
+    void *args[] = {&a};
+    const int grid = (int)std::min<cvg_u64>((cvg_u64)v.occ * r->ctx->n_sm, r->max_tiles);
+    r->grid = std::max(grid, 1);
+    cudaEvent_t e0 = r->ev0, e1 = r->ev1;
+    const bool each = timed && (r->p.flags & CVG_FLAG_TIME_FILL);
+    if (each) {
+        if (r->fill_ev_used == r->fill_ev.size()) {
+            cudaEvent_t x, y;
+            CK(cudaEventCreate(&x));
+            CK(cudaEventCreate(&y));
+            r->fill_ev.emplace_back(x, y);
+        }
+        e0 = r->fill_ev[r->fill_ev_used].first;
+        e1 = r->fill_ev[r->fill_ev_used].second;
+        r->fill_ev_used++;
+    }
+    if (timed) CK(cudaEventRecord(e0, r->ctx->stream));
+    CK(cudaLaunchKernel((const void *)v.kernel, dim3(r->grid), dim3(r->block), args, v.smem,
+                        r->ctx->stream));
+    if (timed) CK(cudaEventRecord(e1, r->ctx->stream));
+    if (each) {   // keep "last fill" queries valid
+        r->ev0 = e0;
+        r->ev1 = e1;
+    }
+    return CVG_OK;
+}
+
+cvg_status enqueue_stages(cvg_run_s *r, int stages, bool timed)
+{
+    cudaStream_t s = r->ctx->stream;
+    if (stages & CVG_STAGE_FILL) {
+        if (r->replay) {
+            cvg_u64 S = 0;   // the replay buffer must cover every sample of this fill
+            CK(cudaMemcpyAsync(&S, r->nh_sum + r->n_cubes, sizeof(S), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (S > r->ubuf_samples)
+                return fail(CVG_ERR_INVALID, "replay uniforms cover " + std::to_string(r->ubuf_samples) +
+                                                 " samples, the fill needs " + std::to_string(S));
+            if (!r->fill_replay.kernel) CKS(prepare_variant(r, true, false, &r->fill_replay));
+            CKS(launch_fill(r, r->fill_replay, timed));
+        } else {
+            CKS(launch_fill(r, r->fill, timed));
+        }
+    }
+    if (stages & CVG_STAGE_REFINE) CK(cvg_launch_refine(refine_args(r), s));
+    if (stages & CVG_STAGE_REALLOC) CK(cvg_launch_realloc(realloc_args(r), s));
+    return CVG_OK;
+}
+
+cvg_status check_status(cvg_run_s *r)
+{
+    cvg_u32 st = 0;
+    CK(cudaMemcpyAsync(&st, r->status, sizeof(st), cudaMemcpyDeviceToHost, r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    if (st & CVG_KSTAT_BAD_TILE)
+        return fail(CVG_ERR_KERNEL, "fill kernel found an inconsistent tile map");
+    return CVG_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char *cvg_last_error(void) { return g_err.c_str(); }
+const char *cvg_version(void) { return CVG_VERSION; }
+
+cvg_status cvg_context_create(int device, void *stream, cvg_context *out)
+{
+    if (!out) return fail(CVG_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(CVG_ERR_INVALID, "no such device");
+    CK(cudaSetDevice(device));
+    auto *c = new cvg_context_s();
+    c->device = device;
+    cudaDeviceProp prop;
+    cudaError_t e = cudaGetDeviceProperties(&prop, device);
+    if (e != cudaSuccess) { delete c; return fail(CVG_ERR_CUDA, cudaGetErrorString(e)); }
+    c->n_sm = prop.multiProcessorCount;
+    c->smem_optin = (int)prop.sharedMemPerBlockOptin;
+    c->cc_major = prop.major;
+    c->cc_minor = prop.minor;
+    char arch[32];
+    std::snprintf(arch, sizeof(arch), "sm_%d%da", prop.major, prop.minor);
+    c->arch = arch;
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete c; return fail(CVG_ERR_CUDA, cudaGetErrorString(e)); }
+        c->own_stream = true;
+    }
+    *out = c;
+    return CVG_OK;
+}
+
+cvg_status cvg_context_destroy(cvg_context ctx)
+{
+    if (!ctx) return CVG_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->libs) cudaLibraryUnload(kv.second);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CVG_OK;
+}
+
+cvg_status cvg_compile_integrand(cvg_context ctx, const char *source, int32_t n_dim, int32_t abi,
+                                 int32_t n_params, int32_t has_grad, cvg_integrand *out)
+{
+    if (!ctx || !source || !out) return fail(CVG_ERR_INVALID, "NULL argument");
+    if (n_dim < 1 || n_dim > 32) return fail(CVG_ERR_INVALID, "n_dim must be in [1, 32]");
+    if (n_params < 0 || n_params > 64) return fail(CVG_ERR_INVALID, "n_params must be in [0, 64]");
+    if (abi != CVG_ABI_NATIVE && abi != CVG_ABI_NUMBA) return fail(CVG_ERR_INVALID, "bad abi");
+    if (abi == CVG_ABI_NUMBA && (n_params || has_grad))
+        return fail(CVG_ERR_INVALID, "numba ABI takes no parameters");
+    auto *f = new cvg_integrand_s();
+    f->ctx = ctx;
+    f->source = source;
+    f->dim = n_dim;
+    f->abi = abi;
+    f->n_params = n_params;
+    f->has_grad = has_grad ? 1 : 0;
+    // Kernels are compiled on first use (run creation), per precision and tile
+    // shape; source errors are reported there with the NVRTC log.
+    *out = f;
+    return CVG_OK;
+}
+
+cvg_status cvg_integrand_release(cvg_integrand f)
+{
+    delete f;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp,
+                          const double *theta, cvg_run *out)
+{
+    if (!ctx || !f || !pp || !out) return fail(CVG_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    const cvg_params &p = *pp;
+    if (p.n_dim != f->dim) return fail(CVG_ERR_INVALID, "n_dim differs from the integrand's");
+    if (p.max_it < 1) return fail(CVG_ERR_INVALID, "max_it must be >= 1");
+    if (p.skip < 0) return fail(CVG_ERR_INVALID, "skip must be >= 0");
+    if (p.tot_eval < 1) return fail(CVG_ERR_INVALID, "tot_eval must be >= 1");
+    if (p.n_intervals < 2 || p.n_intervals > CVG_REFINE_MAX_N)
+        return fail(CVG_ERR_INVALID, "n_intervals must be in [2, 4096]");
+    if (p.precision != CVG_PREC_FP64 && p.precision != CVG_PREC_FP32)
+        return fail(CVG_ERR_INVALID, "precision must be CVG_PREC_FP64 or CVG_PREC_FP32");
+    if (!(p.alpha >= 0.0) || !(p.beta >= 0.0)) return fail(CVG_ERR_INVALID, "alpha, beta >= 0");
+    if (f->n_params > 0 && !theta) return fail(CVG_ERR_INVALID, "integrand needs theta");
+    if (f->abi == CVG_ABI_NUMBA && p.precision != CVG_PREC_FP64)
+        return fail(CVG_ERR_INVALID, "numba ABI integrands are FP64");
+
+    auto *r = new cvg_run_s();
+    r->ctx = ctx;
+    r->f = f;
+    r->p = p;
+    // sizing: src/main.cu:304, 329-331, 337, 444-445
+    r->n_eval_it = p.tot_eval / p.max_it;
+    const int D = f->dim;
+    r->n_strat = p.n_strat > 0 ? p.n_strat : (int)std::pow((double)r->n_eval_it / 4.0, 1.0 / D);
+    if (r->n_strat < 1) { delete r; return fail(CVG_ERR_INVALID, "evals per iteration too small for one stratum (n_strat < 1)"); }
+    const double nc = std::pow((double)r->n_strat, (double)D);
+    if (nc > 4294967295.0) { delete r; return fail(CVG_ERR_INVALID, "n_strat^n_dim exceeds 2^32-1 hypercubes"); }
+    r->n_cubes = (cvg_u32)nc;
+    r->v_cubes = std::pow(1.0 / r->n_strat, (double)D);
+    const cvg_u64 s_max = (cvg_u64)r->n_eval_it + 2ull * r->n_cubes;
+    if (s_max >= (1ull << 31) - (1ull << 20)) {
+        delete r;
+        return fail(CVG_ERR_INVALID, "evals per iteration + 2*n_cubes must stay below 2^31");
+    }
+    const int64_t nh0 = std::max<int64_t>(2, (int64_t)(1.0 / (double)r->n_cubes * (double)r->n_eval_it));
+
+    // tile shape
+    r->block = p.block > 0 ? p.block : 256;
+    r->spt = p.spt > 0 ? p.spt : 8;
+    if (r->block % 32 || r->block > 1024) { delete r; return fail(CVG_ERR_INVALID, "block must be a multiple of 32, <= 1024"); }
+    if (r->spt < 1 || r->spt > 256) { delete r; return fail(CVG_ERR_INVALID, "spt must be in [1, 256]"); }
+    r->TS = r->block * r->spt;
+    r->max_tiles = (s_max + r->TS - 1) / r->TS + 1;
+    r->nb = cvg_realloc_blocks(r->n_cubes);
+    choose_layout(r);
+
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) { delete r; return fail(CVG_ERR_CUDA, cudaGetErrorString(e)); }
+
+    // arena
+    const int N = p.n_intervals;
+    struct seg { void **ptr; size_t bytes; };
+    std::vector<seg> segs = {
+        {(void **)&r->x_edges, sizeof(double) * D * (N + 1)},
+        {(void **)&r->x_edges32, sizeof(float) * D * (N + 1)},
+        {(void **)&r->weights, sizeof(double) * D * N},
+        {(void **)&r->counts, sizeof(cvg_u32) * D * N},
+        {(void **)&r->JF, sizeof(double) * r->n_cubes},
+        {(void **)&r->JF2, sizeof(double) * r->n_cubes},
+        {(void **)&r->dh, sizeof(double) * r->n_cubes},
+        {(void **)&r->nh_sum, sizeof(cvg_u64) * ((size_t)r->n_cubes + 1)},
+        {(void **)&r->nh_new, sizeof(cvg_u32) * r->n_cubes},
+        {(void **)&r->tile_cube, sizeof(cvg_u32) * r->max_tiles},
+        {(void **)&r->partials, sizeof(double) * 3 * r->nb},
+        {(void **)&r->bsums, sizeof(cvg_u64) * (r->nb + 1)},
+        {(void **)&r->stats, sizeof(double) * 3 * p.max_it},
+        {(void **)&r->acc, sizeof(cvg_acc_dev)},
+        {(void **)&r->iteration, sizeof(cvg_u32)},
+        {(void **)&r->status, sizeof(cvg_u32)},
+        {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
+        {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
+    };
+    size_t total = 0;
+    for (auto &s : segs) total += (s.bytes + 255) & ~(size_t)255;
+    e = cudaMalloc(&r->arena, total);
+    if (e != cudaSuccess) {
+        delete r;
+        return fail(CVG_ERR_NOMEM, std::string("cudaMalloc of the run arena (") +
+                                       std::to_string(total >> 20) + " MiB): " + cudaGetErrorString(e));
+    }
+    size_t off = 0;
+    for (auto &s : segs) {
+        *s.ptr = (char *)r->arena + off;
+        off += (s.bytes + 255) & ~(size_t)255;
+    }
+    *out = r;   // from here on cvg_run_destroy cleans up
+
+    cudaStream_t st = ctx->stream;
+    CK(cudaEventCreate(&r->ev0));
+    CK(cudaEventCreate(&r->ev1));
+    r->ev0_own = r->ev0;
+    r->ev1_own = r->ev1;
+    // uniform grid x_j = j/N (src/main.cu:432-441)
+    std::vector<double> xe((size_t)D * (N + 1));
+    const double step = 1.0 / N;
+    for (int d = 0; d < D; ++d)
+        for (int j = 0; j <= N; ++j) xe[(size_t)d * (N + 1) + j] = j * step;
+    CK(cudaMemcpyAsync(r->x_edges, xe.data(), sizeof(double) * xe.size(), cudaMemcpyHostToDevice, st));
+    CK(cvg_launch_grid32(r->x_edges, r->x_edges32, D * (N + 1), st));
+    CK(cudaMemsetAsync(r->weights, 0, sizeof(double) * D * N, st));
+    CK(cudaMemsetAsync(r->counts, 0, sizeof(cvg_u32) * D * N, st));
+    CK(cudaMemsetAsync(r->JF, 0, sizeof(double) * r->n_cubes, st));
+    CK(cudaMemsetAsync(r->JF2, 0, sizeof(double) * r->n_cubes, st));
+    CK(cudaMemsetAsync(r->acc, 0, sizeof(cvg_acc_dev), st));
+    CK(cudaMemsetAsync(r->iteration, 0, sizeof(cvg_u32), st));
+    CK(cudaMemsetAsync(r->status, 0, sizeof(cvg_u32), st));
+    CK(cudaMemsetAsync(r->stats, 0, sizeof(double) * 3 * p.max_it, st));
+    CK(cudaMemsetAsync(r->grad, 0, sizeof(double) * std::max(1, f->n_params), st));
+    if (f->n_params > 0)
+        CK(cudaMemcpyAsync(r->theta, theta, sizeof(double) * f->n_params, cudaMemcpyHostToDevice, st));
+    // nh init (src/main.cu:443-448) -> prefix and tile map
+    CK(cvg_launch_fill_u32(r->nh_new, (cvg_u32)nh0, r->n_cubes, st));
+    CK(cvg_launch_set_nh(realloc_args(r), r->nh_new, st));
+    CKS(prepare_variant(r, false, false, &r->fill));
+    CK(cudaStreamSynchronize(st));
+    return CVG_OK;
+}
+
+cvg_status cvg_run_destroy(cvg_run r)
+{
+    if (!r) return CVG_OK;
+    cudaSetDevice(r->ctx->device);
+    cudaStreamSynchronize(r->ctx->stream);
+    if (r->graph_exec) cudaGraphExecDestroy(r->graph_exec);
+    if (r->graph) cudaGraphDestroy(r->graph);
+    // ev0/ev1 alias either the run's own pair or a pair of fill_ev
+    for (auto &pr : r->fill_ev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    if (r->ev0_own) cudaEventDestroy(r->ev0_own);
+    if (r->ev1_own) cudaEventDestroy(r->ev1_own);
+    if (r->ubuf) cudaFree(r->ubuf);
+    if (r->arena) cudaFree(r->arena);
+    delete r;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_step(cvg_run r, int32_t stages)
+{
+    if (!r) return fail(CVG_ERR_INVALID, "NULL run");
+    CK(cudaSetDevice(r->ctx->device));
+    if ((stages & CVG_STAGE_REALLOC) && r->it_done >= r->p.max_it)
+        return fail(CVG_ERR_STATE, "all max_it iterations are done");
+    CKS(enqueue_stages(r, stages, (stages & CVG_STAGE_FILL) != 0));
+    if (stages & CVG_STAGE_REALLOC) r->it_done++;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_iterate(cvg_run r, int32_t n)
+{
+    if (!r) return fail(CVG_ERR_INVALID, "NULL run");
+    if (n < 0 || r->it_done + n > r->p.max_it)
+        return fail(CVG_ERR_STATE, "iterations beyond max_it");
+    CK(cudaSetDevice(r->ctx->device));
+    const int all = CVG_STAGE_FILL | CVG_STAGE_REFINE | CVG_STAGE_REALLOC;
+    if ((r->p.flags & CVG_FLAG_GRAPH) && !r->replay) {
+        if (!r->graph_exec) {
+            cudaStream_t s = r->ctx->stream;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            cvg_status st = enqueue_stages(r, all, false);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (st != CVG_OK) { if (g) cudaGraphDestroy(g); return st; }
+            CK(e);
+            r->graph = g;
+            CK(cudaGraphInstantiate(&r->graph_exec, g, 0));
+        }
+        for (int i = 0; i < n; ++i) CK(cudaGraphLaunch(r->graph_exec, r->ctx->stream));
+    } else {
+        const bool each = (r->p.flags & CVG_FLAG_TIME_FILL) != 0;
+        for (int i = 0; i < n; ++i) CKS(enqueue_stages(r, all, each || i == n - 1));
+    }
+    r->it_done += n;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_sync(cvg_run r)
+{
+    if (!r) return fail(CVG_ERR_INVALID, "NULL run");
+    CK(cudaSetDevice(r->ctx->device));
+    return check_status(r);
+}
+
+cvg_status cvg_run_result(cvg_run r, cvg_result *out, double *it_res, double *it_sig2)
+{
+    if (!r || !out) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaSetDevice(r->ctx->device));
+    cvg_acc_dev acc;
+    const int M = r->p.max_it;
+    std::vector<double> stats(2 * (size_t)M);
+    CK(cudaMemcpyAsync(&acc, r->acc, sizeof(acc), cudaMemcpyDeviceToHost, r->ctx->stream));
+    CK(cudaMemcpyAsync(stats.data(), r->stats, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost,
+                       r->ctx->stream));
+    CKS(check_status(r));
+    std::memset(out, 0, sizeof(*out));
+    // weighted mean over iterations >= skip (src/main.cu:698-714), error
+    // 1/sqrt(sum 1/sigma^2) (src/main.cu:792); chi^2 two-pass on the host.
+    const int done = std::min(r->it_done, M);
+    double sw = 0.0, swr = 0.0;
+    int used = 0;
+    for (int i = r->p.skip; i < done; ++i) {
+        sw += 1.0 / stats[M + i];
+        swr += stats[i] / stats[M + i];
+        ++used;
+    }
+    out->result = used ? swr / sw : 0.0;
+    out->error = used ? 1.0 / std::sqrt(sw) : 0.0;
+    double chi2 = 0.0;
+    for (int i = r->p.skip; i < done; ++i) {
+        const double dlt = stats[i] - out->result;
+        chi2 += dlt * dlt / stats[M + i];
+    }
+    out->chi2_dof = used > 1 ? chi2 / (used - 1) : 0.0;
+    out->n_strat = r->n_strat;
+    out->n_intervals = r->p.n_intervals;
+    out->n_cubes = r->n_cubes;
+    out->tot_nevals = (int64_t)acc.tot_nevals;
+    out->seed = r->p.seed;
+    out->gpu_thr = r->p.gpu_thr;
+    out->n_it_used = used;
+    out->n_it_done = done;
+    out->precision = r->p.precision;
+    if (it_res) for (int i = 0; i < M; ++i) it_res[i] = stats[i];
+    if (it_sig2) for (int i = 0; i < M; ++i) it_sig2[i] = stats[M + i];
+    return CVG_OK;
+}
+
+cvg_status cvg_integrate(cvg_context ctx, cvg_integrand f, const cvg_params *p,
+                         const double *theta, cvg_result *out, double *it_res, double *it_sig2)
+{
+    if (!out) return fail(CVG_ERR_INVALID, "out is NULL");
+    const double t0 = now_ms();
+    cvg_run r = nullptr;
+    cvg_status s = cvg_run_create(ctx, f, p, theta, &r);
+    if (s != CVG_OK) { cvg_run_destroy(r); return s; }
+    const double t1 = now_ms();
+    s = cvg_run_iterate(r, p->max_it);
+    if (s == CVG_OK) s = cvg_run_result(r, out, it_res, it_sig2);
+    const double t2 = now_ms();
+    cvg_run_destroy(r);
+    out->tot_time_ms = now_ms() - t0;
+    out->avg_it_time_ms = (t2 - t1) / p->max_it;
+    return s;
+}
+
+cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
+{
+    if (!r || !host) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaSetDevice(r->ctx->device));
+    const int D = r->f->dim, N = r->p.n_intervals;
+    const void *src = nullptr;
+    size_t need = 0;
+    switch (buf) {
+    case CVG_BUF_X_EDGES: src = r->x_edges; need = sizeof(double) * D * (N + 1); break;
+    case CVG_BUF_NH: {
+        std::vector<cvg_u64> ps((size_t)r->n_cubes + 1);
+        need = sizeof(cvg_u32) * r->n_cubes;
+        if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch");
+        CK(cudaMemcpyAsync(ps.data(), r->nh_sum, sizeof(cvg_u64) * ps.size(), cudaMemcpyDeviceToHost, r->ctx->stream));
+        CK(cudaStreamSynchronize(r->ctx->stream));
+        cvg_u32 *o = (cvg_u32 *)host;
+        for (size_t c = 0; c < r->n_cubes; ++c) o[c] = (cvg_u32)(ps[c + 1] - ps[c]);
+        return CVG_OK;
+    }
+    case CVG_BUF_NH_SUM: src = r->nh_sum; need = sizeof(cvg_u64) * ((size_t)r->n_cubes + 1); break;
+    case CVG_BUF_JF: src = r->JF; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_JF2: src = r->JF2; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_WEIGHTS: src = r->weights; need = sizeof(double) * D * N; break;
+    case CVG_BUF_COUNTS: src = r->counts; need = sizeof(cvg_u32) * D * N; break;
+    case CVG_BUF_DH: src = r->dh; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_THETA: src = r->theta; need = sizeof(double) * r->f->n_params; break;
+    case CVG_BUF_ITERATION: src = r->iteration; need = sizeof(cvg_u32); break;
+    case CVG_BUF_STATS: src = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
+    default: return fail(CVG_ERR_INVALID, "unknown buffer");
+    }
+    if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
+    CK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    return CVG_OK;
+}
+
+cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes)
+{
+    if (!r) return fail(CVG_ERR_INVALID, "NULL run");
+    CK(cudaSetDevice(r->ctx->device));
+    const int D = r->f->dim, N = r->p.n_intervals;
+    cudaStream_t st = r->ctx->stream;
+    void *dst = nullptr;
+    size_t need = 0;
+    switch (buf) {
+    case CVG_BUF_X_EDGES: dst = r->x_edges; need = sizeof(double) * D * (N + 1); break;
+    case CVG_BUF_NH: {
+        need = sizeof(cvg_u32) * r->n_cubes;
+        if (!host || bytes != need) return fail(CVG_ERR_INVALID, "size mismatch");
+        const cvg_u32 *nh = (const cvg_u32 *)host;
+        cvg_u64 tot = 0;
+        for (size_t c = 0; c < r->n_cubes; ++c) {
+            if (nh[c] < 2) return fail(CVG_ERR_INVALID, "every hypercube needs >= 2 samples");
+            tot += nh[c];
+        }
+        if (tot > (cvg_u64)(r->max_tiles - 1) * r->TS)
+            return fail(CVG_ERR_INVALID, "sum of nh exceeds evals/iteration + 2*n_cubes");
+        CK(cvg_launch_set_nh(realloc_args(r), nh, st));
+        CK(cudaStreamSynchronize(st));
+        return CVG_OK;
+    }
+    case CVG_BUF_JF: dst = r->JF; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_JF2: dst = r->JF2; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_WEIGHTS: dst = r->weights; need = sizeof(double) * D * N; break;
+    case CVG_BUF_COUNTS: dst = r->counts; need = sizeof(cvg_u32) * D * N; break;
+    case CVG_BUF_THETA: dst = r->theta; need = sizeof(double) * r->f->n_params; break;
+    case CVG_BUF_ITERATION: dst = r->iteration; need = sizeof(cvg_u32); break;
+    case CVG_BUF_UNIFORMS: {
+        if (bytes == 0) { r->replay = false; return CVG_OK; }
+        if (!host || bytes % (sizeof(float) * D)) return fail(CVG_ERR_INVALID, "uniforms: [S][dim] floats");
+        const size_t ns = bytes / (sizeof(float) * D);
+        if (ns > r->ubuf_samples) {
+            if (r->ubuf) CK(cudaFree(r->ubuf));
+            r->ubuf = nullptr;
+            r->ubuf_samples = 0;
+            CK(cudaMalloc(&r->ubuf, bytes));
+            r->ubuf_samples = ns;
+        }
+        CK(cudaMemcpyAsync(r->ubuf, host, bytes, cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));
+        r->replay = true;
+        return CVG_OK;
+    }
+    default: return fail(CVG_ERR_INVALID, "buffer not settable");
+    }
+    if (!host || bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
+    CK(cudaMemcpyAsync(dst, host, need, cudaMemcpyHostToDevice, st));
+    if (buf == CVG_BUF_X_EDGES) CK(cvg_launch_grid32(r->x_edges, r->x_edges32, D * (N + 1), st));
+    CK(cudaStreamSynchronize(st));
+    return CVG_OK;
+}
+
+cvg_status cvg_run_info_get(cvg_run r, cvg_run_info *o)
+{
+    if (!r || !o) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaSetDevice(r->ctx->device));
+    cvg_u64 S = 0;
+    CK(cudaMemcpyAsync(&S, r->nh_sum + r->n_cubes, sizeof(S), cudaMemcpyDeviceToHost, r->ctx->stream));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    std::memset(o, 0, sizeof(*o));
+    o->n_eval_it = r->n_eval_it;
+    o->n_cubes = r->n_cubes;
+    o->next_samples = (int64_t)S;
+    o->max_tiles = (int64_t)r->max_tiles;
+    o->n_strat = r->n_strat;
+    o->n_intervals = r->p.n_intervals;
+    o->n_dim = r->f->dim;
+    o->block = r->block;
+    o->spt = r->spt;
+    o->grid = (int32_t)std::min<cvg_u64>((cvg_u64)r->fill.occ * r->ctx->n_sm, r->max_tiles);
+    o->edges_smem = r->esm;
+    o->hist_smem = r->hsm;
+    o->v_cubes = r->v_cubes;
+    o->fill_smem_bytes = (int64_t)r->fill.smem;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_grad(cvg_run r, uint32_t it, double *grad)
+{
+    if (!r || !grad) return fail(CVG_ERR_INVALID, "NULL argument");
+    if (!r->f->has_grad || r->f->n_params < 1)
+        return fail(CVG_ERR_INVALID, "integrand has no integrand_grad / parameters");
+    CK(cudaSetDevice(r->ctx->device));
+    if (!r->gradk.kernel) CKS(prepare_variant(r, false, true, &r->gradk));
+    cudaStream_t st = r->ctx->stream;
+    cvg_u32 saved = 0;
+    if (it != 0xFFFFFFFFu) {
+        CK(cudaMemcpyAsync(&saved, r->iteration, sizeof(saved), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMemcpyAsync(r->iteration, &it, sizeof(it), cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaMemsetAsync(r->grad, 0, sizeof(double) * r->f->n_params, st));
+    CKS(launch_fill(r, r->gradk, false));
+    CK(cudaMemcpyAsync(grad, r->grad, sizeof(double) * r->f->n_params, cudaMemcpyDeviceToHost, st));
+    if (it != 0xFFFFFFFFu)
+        CK(cudaMemcpyAsync(r->iteration, &saved, sizeof(saved), cudaMemcpyHostToDevice, st));
+    return check_status(r);
+}
+
+cvg_status cvg_run_fill_times(cvg_run r, float *ms, int32_t cap, int32_t *n)
+{
+    if (!r || !n) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaSetDevice(r->ctx->device));
+    CK(cudaStreamSynchronize(r->ctx->stream));
+    int32_t k = 0;
+    for (size_t i = 0; i < r->fill_ev_used; ++i) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, r->fill_ev[i].first, r->fill_ev[i].second));
+        if (ms && k < cap) ms[k] = t;
+        ++k;
+    }
+    *n = k;
+    r->fill_ev_used = 0;
+    return CVG_OK;
+}
+
+cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out)
+{
+    if (!ctx || !out) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best = 1e30f;
+    if (kind == 0 || kind == 1) {
+        double *sink = nullptr;
+        CK(cudaMalloc(&sink, sizeof(double)));
+        const int blocks = ctx->n_sm * 8;
+        const int iters = kind == 0 ? 4096 : 256;
+        for (int rep = 0; rep < 4; ++rep) {
+            CK(cudaEventRecord(a, s));
+            CK(cvg_launch_fma_bench(kind, blocks, iters, sink, s));
+            CK(cudaEventRecord(b, s));
+            CK(cudaEventSynchronize(b));
+            float t;
+            CK(cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) best = std::min(best, t);
+        }
+        cudaFree(sink);
+        const double flops = 2.0 * 8.0 * iters * 256.0 * blocks;
+        *out = flops / (best * 1e-3) / 1e12;
+    } else if (kind == 2) {
+        const size_t bytes = (size_t)1 << 30;
+        void *x = nullptr, *y = nullptr;
+        CK(cudaMalloc(&x, bytes));
+        cudaError_t e = cudaMalloc(&y, bytes);
+        if (e != cudaSuccess) { cudaFree(x); return fail(CVG_ERR_NOMEM, cudaGetErrorString(e)); }
+        CK(cudaMemsetAsync(x, 0, bytes, s));
+        for (int rep = 0; rep < 6; ++rep) {
+            CK(cudaEventRecord(a, s));
+            CK(cvg_launch_copy_bench((const float4 *)x, (float4 *)y, bytes / 16, s));
+            CK(cudaEventRecord(b, s));
+            CK(cudaEventSynchronize(b));
+            float t;
+            CK(cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) best = std::min(best, t);
+        }
+        cudaFree(x);
+        cudaFree(y);
+        *out = 2.0 * bytes / (best * 1e-3) / 1e9;
+    } else {
+        return fail(CVG_ERR_INVALID, "kind must be 0, 1 or 2");
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return CVG_OK;
+}
+
+cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int32_t n_params,
+                             int32_t has_grad, int32_t precision, const char *arch, char *log,
+                             size_t log_len)
+{
+    if (!source || !arch) return fail(CVG_ERR_INVALID, "NULL argument");
+    if (n_dim < 1 || n_dim > 32) return fail(CVG_ERR_INVALID, "n_dim must be in [1, 32]");
+    cvg_integrand_s f;
+    f.source = source;
+    f.dim = n_dim;
+    f.abi = abi;
+    f.n_params = n_params;
+    f.has_grad = has_grad;
+    std::string all;
+    cvg_status st = CVG_OK;
+    for (int g = 0; g <= (has_grad ? 1 : 0) && st == CVG_OK; ++g) {
+        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi};
+        std::vector<char> cubin;
+        std::string l;
+        st = nvrtc_cubin(make_source(f, k), nvrtc_options(arch), cubin, l);
+        all += l;
+    }
+    if (log && log_len) {
+        std::strncpy(log, all.c_str(), log_len - 1);
+        log[log_len - 1] = '\0';
+    }
+    return st;
+}
+
+cvg_status cvg_run_last_fill_ms(cvg_run r, float *ms)
+{
+    if (!r || !ms) return fail(CVG_ERR_INVALID, "NULL argument");
+    CK(cudaEventSynchronize(r->ev1));
+    CK(cudaEventElapsedTime(ms, r->ev0, r->ev1));
+    return CVG_OK;
+}
+
+}  // extern "C"

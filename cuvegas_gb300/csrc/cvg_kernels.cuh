@@ -1,0 +1,81 @@
+// cvg_kernels.cuh -- argument blocks and launch wrappers of the precompiled
+// reallocation (K3) and grid-refinement (K4) kernels.
+#ifndef CVG_KERNELS_CUH
+#define CVG_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include "cvg_common.cuh"
+
+// Per-iteration statistics kept on the device (no host sync per iteration).
+// stats[0..max_it)        : I_it   (sum of per-cube estimates)
+// stats[max_it..2*max_it) : sigma2_it (sum of per-cube variances / nh)
+// stats[2*max_it..3*max_it): samples of iteration it
+// acc                     : running sums of the weighted mean
+struct cvg_acc_dev {
+    double sw;        // sum 1/sigma2
+    double swr;       // sum I/sigma2
+    double swr2;      // sum I^2/sigma2
+    double dh_sum;    // sum of damped cube variances of the last iteration
+    cvg_u64 used;     // iterations in the mean
+    cvg_u64 tot_nevals;
+    cvg_u64 last_nevals;
+    cvg_u64 pad;
+};
+
+struct cvg_realloc_args {
+    cvg_u64 *nh_sum;        // [n_cubes+1], read (old), rewritten (new)
+    double *JF, *JF2;       // [n_cubes], read then zeroed
+    double *dh;             // [n_cubes]
+    cvg_u32 *nh_new;        // [n_cubes]
+    double *partials;       // [n_blocks][3]
+    cvg_u64 *bsums;         // [n_blocks]
+    cvg_u32 *tile_cube;     // [max_tiles]
+    double *stats;          // [2*max_it]
+    cvg_acc_dev *acc;
+    cvg_u32 *iteration;
+    cvg_u32 *status;
+    cvg_u64 max_tiles;
+    cvg_i64 n_eval_it;
+    double v_cubes;
+    double beta;
+    cvg_u32 n_cubes;
+    int tile_samples;
+    int skip;
+    int max_it;
+    int fast_pow;           // 1: d_h^beta through FP32 log2/exp2 (FP32 form)
+    int adapt;              // 0: keep nh (no reallocation), still accumulate results
+};
+
+struct cvg_refine_args {
+    double *x_edges;        // [dim][N+1]
+    float *x_edges32;       // [dim][N+1]
+    double *weights;        // [dim][N], read then zeroed
+    cvg_u32 *counts;        // [dim][N], read then zeroed
+    double alpha;
+    int dim;
+    int n_intervals;
+    int adapt;              // 0: only clear the histograms
+};
+
+enum { CVG_REALLOC_CHUNK = 2048, CVG_REFINE_BLOCK = 1024, CVG_REFINE_MAX_N = 4096 };
+
+inline unsigned cvg_realloc_blocks(cvg_u32 n_cubes)
+{
+    return (unsigned)((n_cubes + CVG_REALLOC_CHUNK - 1) / CVG_REALLOC_CHUNK);
+}
+
+// Launch the reallocation chain (results, finish, count, scan, apply).
+cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s);
+// Launch the refinement (one CTA per dimension).
+cudaError_t cvg_launch_refine(const cvg_refine_args &a, cudaStream_t s);
+// Tile map + prefix from an explicit nh (state import / initialisation).
+cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cudaStream_t s);
+// FP32 copy of the grid.
+cudaError_t cvg_launch_grid32(const double *x, float *x32, int n, cudaStream_t s);
+// Peak-throughput microbenchmarks (FP32 / FP64 FMA chains, device copy).
+cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, cudaStream_t s);
+cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cudaStream_t s);
+// Fill n words with a value.
+cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
+
+#endif

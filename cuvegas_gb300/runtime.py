@@ -1,0 +1,243 @@
+"""Object layer over the C ABI: contexts, compiled integrands, runs.
+
+All work happens in libcuvegas.so on the GPU; this module only moves
+parameters and host arrays across the boundary.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+_contexts = {}
+
+
+class Context:
+    """One device + stream (include/cuvegas.h: cvg_context_create)."""
+
+    def __init__(self, device=0, stream=None):
+        self._lib = L.load()
+        h = C.c_void_p()
+        L.check(self._lib.cvg_context_create(int(device), stream, C.byref(h)))
+        self.handle = h
+        self.device = device
+        self._integrands = {}
+
+    def close(self):
+        if self.handle:
+            for f in list(self._integrands.values()):
+                f.close()
+            self._integrands.clear()
+            self._lib.cvg_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def measure_peak(self, kind):
+        v = C.c_double()
+        L.check(self._lib.cvg_measure_peak(self.handle, int(kind), C.byref(v)))
+        return v.value
+
+    def integrand(self, source, n_dim, n_params=0, has_grad=False, abi=L.ABI_NATIVE):
+        key = (source, int(n_dim), int(n_params), bool(has_grad), int(abi))
+        f = self._integrands.get(key)
+        if f is None:
+            f = Integrand(self, source, n_dim, n_params, has_grad, abi)
+            self._integrands[key] = f
+        return f
+
+
+def default_context(device=None):
+    if device is None:
+        device = 0
+        try:
+            import torch
+            if torch.cuda.is_available():
+                device = torch.cuda.current_device()
+        except Exception:
+            pass
+    ctx = _contexts.get(device)
+    if ctx is None or not ctx.handle:
+        ctx = Context(device)
+        _contexts[device] = ctx
+    return ctx
+
+
+class Integrand:
+    """A JIT-compiled integrand (cvg_compile_integrand)."""
+
+    def __init__(self, ctx, source, n_dim, n_params=0, has_grad=False, abi=L.ABI_NATIVE):
+        self.ctx = ctx
+        self.n_dim = int(n_dim)
+        self.n_params = int(n_params)
+        self.has_grad = bool(has_grad)
+        h = C.c_void_p()
+        L.check(ctx._lib.cvg_compile_integrand(ctx.handle, source.encode(), self.n_dim, int(abi),
+                                               self.n_params, int(self.has_grad), C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.ctx._lib.cvg_integrand_release(self.handle)
+            self.handle = None
+
+
+def make_params(n_dim, tot_eval, max_it, skip=5, n_intervals=1024, n_strat=0, alpha=0.5,
+                beta=0.75, seed=0, precision=L.PREC_FP64, flags=0, block=0, spt=0, instance=0,
+                max_batch_size=1048576, gpu_thr=0.1):
+    p = L.Params()
+    p.tot_eval = int(tot_eval)
+    p.max_it = int(max_it)
+    p.skip = int(skip)
+    p.max_batch_size = int(max_batch_size)
+    p.n_intervals = int(n_intervals)
+    p.n_strat = int(n_strat or 0)
+    p.n_dim = int(n_dim)
+    p.precision = int(precision)
+    p.alpha = float(alpha)
+    p.beta = float(beta)
+    p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    p.gpu_thr = float(gpu_thr)
+    p.flags = int(flags)
+    p.block = int(block)
+    p.spt = int(spt)
+    p.instance = int(instance)
+    return p
+
+
+def _theta_ptr(theta, n_params):
+    if n_params == 0:
+        return None, None
+    th = np.ascontiguousarray(theta, dtype=np.float64)
+    if th.size != n_params:
+        raise ValueError("theta must have %d values" % n_params)
+    return th, th.ctypes.data_as(C.c_void_p)
+
+
+def integrate_once(integrand, params, theta=None):
+    """cvg_integrate: one whole integration; returns (Result, it_res, it_sig2)."""
+    lib = integrand.ctx._lib
+    th, thp = _theta_ptr(theta, integrand.n_params)
+    res = L.Result()
+    it_res = np.zeros(params.max_it)
+    it_sig = np.zeros(params.max_it)
+    L.check(lib.cvg_integrate(integrand.ctx.handle, integrand.handle, C.byref(params), thp,
+                              C.byref(res), it_res.ctypes.data_as(C.c_void_p),
+                              it_sig.ctypes.data_as(C.c_void_p)))
+    return res, it_res, it_sig
+
+
+_BUF_DTYPES = {
+    L.BUF_X_EDGES: np.float64, L.BUF_NH: np.uint32, L.BUF_NH_SUM: np.uint64,
+    L.BUF_JF: np.float64, L.BUF_JF2: np.float64, L.BUF_WEIGHTS: np.float64,
+    L.BUF_COUNTS: np.uint32, L.BUF_DH: np.float64, L.BUF_THETA: np.float64,
+    L.BUF_ITERATION: np.uint32, L.BUF_STATS: np.float64,
+}
+
+
+class Run:
+    """Persistent device state of one integration (cvg_run_*)."""
+
+    def __init__(self, integrand, params, theta=None):
+        self.f = integrand
+        self.params = params
+        self._lib = integrand.ctx._lib
+        th, thp = _theta_ptr(theta, integrand.n_params)
+        h = C.c_void_p()
+        L.check(self._lib.cvg_run_create(integrand.ctx.handle, integrand.handle, C.byref(params),
+                                         thp, C.byref(h)))
+        self.handle = h
+        self.info = self.get_info()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.cvg_run_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def get_info(self):
+        info = L.RunInfo()
+        L.check(self._lib.cvg_run_info_get(self.handle, C.byref(info)))
+        return info
+
+    def iterate(self, n):
+        L.check(self._lib.cvg_run_iterate(self.handle, int(n)))
+
+    def step(self, stages):
+        L.check(self._lib.cvg_run_step(self.handle, int(stages)))
+
+    def sync(self):
+        L.check(self._lib.cvg_run_sync(self.handle))
+
+    def result(self):
+        res = L.Result()
+        M = self.params.max_it
+        it_res = np.zeros(M)
+        it_sig = np.zeros(M)
+        L.check(self._lib.cvg_run_result(self.handle, C.byref(res),
+                                         it_res.ctypes.data_as(C.c_void_p),
+                                         it_sig.ctypes.data_as(C.c_void_p)))
+        return res, it_res, it_sig
+
+    def _count(self, buf):
+        info = self.get_info()
+        D, N, nc = info.n_dim, info.n_intervals, info.n_cubes
+        return {L.BUF_X_EDGES: D * (N + 1), L.BUF_NH: nc, L.BUF_NH_SUM: nc + 1, L.BUF_JF: nc,
+                L.BUF_JF2: nc, L.BUF_WEIGHTS: D * N, L.BUF_COUNTS: D * N, L.BUF_DH: nc,
+                L.BUF_THETA: self.f.n_params, L.BUF_ITERATION: 1,
+                L.BUF_STATS: 3 * self.params.max_it}[buf]
+
+    def get(self, buf):
+        dt = _BUF_DTYPES[buf]
+        out = np.zeros(self._count(buf), dtype=dt)
+        L.check(self._lib.cvg_run_get(self.handle, int(buf), out.ctypes.data_as(C.c_void_p),
+                                      out.nbytes))
+        if buf in (L.BUF_X_EDGES,):
+            out = out.reshape(self.info.n_dim, self.info.n_intervals + 1)
+        elif buf in (L.BUF_WEIGHTS, L.BUF_COUNTS):
+            out = out.reshape(self.info.n_dim, self.info.n_intervals)
+        elif buf == L.BUF_STATS:
+            out = out.reshape(3, self.params.max_it)
+        return out
+
+    def set(self, buf, arr):
+        if buf == L.BUF_UNIFORMS:
+            if arr is None:
+                L.check(self._lib.cvg_run_set(self.handle, int(buf), None, 0))
+                return
+            a = np.ascontiguousarray(arr, dtype=np.float32)
+        else:
+            a = np.ascontiguousarray(arr, dtype=_BUF_DTYPES[buf]).ravel()
+        L.check(self._lib.cvg_run_set(self.handle, int(buf), a.ctypes.data_as(C.c_void_p),
+                                      a.nbytes))
+
+    def grad(self, it=L.IT_CURRENT):
+        g = np.zeros(self.f.n_params)
+        L.check(self._lib.cvg_run_grad(self.handle, int(it), g.ctypes.data_as(C.c_void_p)))
+        return g
+
+    def fill_times(self, cap=4096):
+        ms = (C.c_float * cap)()
+        n = C.c_int32()
+        L.check(self._lib.cvg_run_fill_times(self.handle, ms, cap, C.byref(n)))
+        return np.array(ms[:min(n.value, cap)], dtype=np.float64)
+
+    def last_fill_ms(self):
+        ms = C.c_float()
+        L.check(self._lib.cvg_run_last_fill_ms(self.handle, C.byref(ms)))
+        return ms.value

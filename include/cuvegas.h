@@ -1,0 +1,193 @@
+/*
+ * cuvegas.h -- C ABI of the GB300-native VEGAS+ integrator (libcuvegas.so).
+ *
+ * Plain pointers, sizes and status codes; no C++ or PyTorch types.  One
+ * process, one GPU.  Each entry point names the reference interface it
+ * replaces (paths relative to the emiliantolo/cuvegas project root).
+ *
+ * Threading: a cvg_context and everything created from it may be used by one
+ * host thread at a time.  Errors never terminate the process (the reference
+ * calls exit(), src/commons/common.cuh:39-45); they return a status and leave
+ * a message readable with cvg_last_error() on the calling thread.
+ */
+#ifndef CUVEGAS_H
+#define CUVEGAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CVG_OK = 0,
+    CVG_ERR_INVALID = 1,    /* bad argument or size                         */
+    CVG_ERR_CUDA = 2,       /* CUDA runtime error                           */
+    CVG_ERR_COMPILE = 3,    /* NVRTC could not compile the integrand source */
+    CVG_ERR_NOMEM = 4,      /* device or host allocation failed             */
+    CVG_ERR_KERNEL = 5,     /* a kernel reported an inconsistent state      */
+    CVG_ERR_STATE = 6       /* call out of order (e.g. past max_it)         */
+} cvg_status;
+
+enum { CVG_PREC_FP64 = 0, CVG_PREC_FP32 = 1 };
+
+/* Integrand source conventions (cvg_compile_integrand `abi`). */
+enum {
+    CVG_ABI_NATIVE = 0,     /* T integrand(T* x) [, const T* theta]; T = double or float   */
+    CVG_ABI_NUMBA = 1       /* int integrand(double* ret, double* x): the device ABI the
+                               reference links (vegas_cuda_extension/cuda_kernel.cu:7) */
+};
+
+/* cvg_params.flags */
+enum {
+    CVG_FLAG_GRAPH = 1,     /* capture one iteration as a CUDA graph and replay it       */
+    CVG_FLAG_NO_ADAPT = 2,  /* keep grid and nh fixed (evaluation with a trained map)    */
+    CVG_FLAG_TIME_FILL = 4  /* time every fill launch with CUDA events (eager iterations)  */
+};
+
+/* Run parameters.  Meanings follow the reference: src/config.cuh:7-26 and
+ * vegas_cuda/src/vegas_cuda_extension/python_wrapper.py:9. */
+typedef struct {
+    int64_t tot_eval;        /* total evaluations over all iterations (tot_eval / n_evals)    */
+    int32_t max_it;          /* iterations                                                   */
+    int32_t skip;            /* iterations left out of the weighted mean                     */
+    int64_t max_batch_size;  /* accepted for compatibility; the fill is persistent           */
+    int32_t n_intervals;     /* bins per dimension of the adaptive grid (nbins)              */
+    int32_t n_strat;         /* strata per dimension; 0 = (int)pow(N_it/4, 1/dim)            */
+    int32_t n_dim;           /* dimension (must equal the compiled integrand's)              */
+    int32_t precision;       /* CVG_PREC_FP64 (plain) or CVG_PREC_FP32 (compensated)         */
+    double alpha;            /* grid damping                                                 */
+    double beta;             /* stratification damping                                       */
+    uint64_t seed;           /* Philox key                                                   */
+    double gpu_thr;          /* accepted for compatibility; no CPU mapping fallback exists   */
+    int32_t flags;           /* CVG_FLAG_*                                                   */
+    int32_t block;           /* fill threads per CTA; 0 = tuned default                      */
+    int32_t spt;             /* fill samples per thread; 0 = tuned default                   */
+    uint32_t instance;       /* Philox stream id (independent integrals)                     */
+} cvg_params;
+
+/* Result record.  First fields mirror the 14-tuple of the reference's
+ * integrate_cuda (vegas_cuda/src/vegas_cuda_extension/cuda_wrapper.cu:869). */
+typedef struct {
+    double result;           /* weighted mean over iterations >= skip                        */
+    double error;            /* 1/sqrt(sum 1/sigma^2)                                        */
+    int32_t n_strat;
+    int32_t n_intervals;
+    int64_t n_cubes;
+    int64_t tot_nevals;      /* integrand evaluations over all iterations                    */
+    double tot_time_ms;      /* wall time of the call                                        */
+    double avg_it_time_ms;   /* iteration-loop wall time / iterations                        */
+    uint64_t seed;
+    double gpu_thr;
+    double chi2_dof;         /* chi^2 per degree of freedom of the iteration estimates       */
+    int32_t n_it_used;
+    int32_t n_it_done;
+    int32_t precision;
+    int32_t pad;
+} cvg_result;
+
+typedef struct cvg_context_s *cvg_context;
+typedef struct cvg_integrand_s *cvg_integrand;
+typedef struct cvg_run_s *cvg_run;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *cvg_last_error(void);
+/* Library version string. */
+const char *cvg_version(void);
+
+/* Context on `device` (replaces the per-call device setup of
+ * cuda_wrapper.cu:292-329).  `stream` may be NULL (the context creates one)
+ * or a cudaStream_t owned by the caller. */
+cvg_status cvg_context_create(int device, void *stream, cvg_context *out);
+cvg_status cvg_context_destroy(cvg_context ctx);
+
+/* JIT-compile an integrand from CUDA C++ source (replaces numba PTX + the
+ * cuLink step, python_wrapper.py:48-61 and cuda_wrapper.cu:221-286).  The
+ * source defines `integrand` per `abi`; `n_params` > 0 means it also takes a
+ * `const T* theta`; `has_grad` means it defines
+ * `void integrand_grad(T* x, const T* theta, T* g)` (dF/dtheta).  Kernels are
+ * compiled lazily per (precision, tile shape) and cached. */
+cvg_status cvg_compile_integrand(cvg_context ctx, const char *source, int32_t n_dim,
+                                 int32_t abi, int32_t n_params, int32_t has_grad,
+                                 cvg_integrand *out);
+cvg_status cvg_integrand_release(cvg_integrand f);
+
+/* Whole integration, the drop-in for integrate_cuda
+ * (cuda_wrapper.cu:290-872): host parameters in, host result out.
+ * `theta` (host, n_params doubles) may be NULL when n_params == 0.
+ * it_res / it_sig2 (host, max_it doubles each) may be NULL. */
+cvg_status cvg_integrate(cvg_context ctx, cvg_integrand f, const cvg_params *p,
+                         const double *theta, cvg_result *out, double *it_res,
+                         double *it_sig2);
+
+/* ---- step-level API (persistent device state; tests, benchmarks, autograd) ---- */
+
+cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *p,
+                          const double *theta, cvg_run *out);
+cvg_status cvg_run_destroy(cvg_run r);
+/* Enqueue n full iterations (fill, reallocation, refinement) on the context
+ * stream; no host synchronisation. */
+cvg_status cvg_run_iterate(cvg_run r, int32_t n);
+/* Stages of one iteration, for step-by-step checks. */
+enum { CVG_STAGE_FILL = 1, CVG_STAGE_REALLOC = 2, CVG_STAGE_REFINE = 4 };
+cvg_status cvg_run_step(cvg_run r, int32_t stages);
+/* Synchronise and summarise the iterations done so far. */
+cvg_status cvg_run_result(cvg_run r, cvg_result *out, double *it_res, double *it_sig2);
+cvg_status cvg_run_sync(cvg_run r);
+
+/* Buffers readable / writable through cvg_run_get / cvg_run_set (host side). */
+enum {
+    CVG_BUF_X_EDGES = 0,     /* double [dim][N+1]        get/set                  */
+    CVG_BUF_NH = 1,          /* uint32 [n_cubes]         get/set (set rebuilds the prefix) */
+    CVG_BUF_NH_SUM = 2,      /* uint64 [n_cubes+1]       get                      */
+    CVG_BUF_JF = 3,          /* double [n_cubes]         get/set                  */
+    CVG_BUF_JF2 = 4,         /* double [n_cubes]         get/set                  */
+    CVG_BUF_WEIGHTS = 5,     /* double [dim][N]          get/set                  */
+    CVG_BUF_COUNTS = 6,      /* uint32 [dim][N]          get/set                  */
+    CVG_BUF_DH = 7,          /* double [n_cubes]         get                      */
+    CVG_BUF_THETA = 8,       /* double [n_params]        get/set                  */
+    CVG_BUF_ITERATION = 9,   /* uint32 [1]               get/set                  */
+    CVG_BUF_UNIFORMS = 10,   /* float  [S][dim]          set: replay these uniforms in
+                                the next fills instead of Philox (parity tests); 0 bytes
+                                switches back                                         */
+    CVG_BUF_STATS = 11       /* double [3][max_it]       get: I_it, sigma2_it, samples_it */
+};
+cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
+cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);
+
+/* Sizes of the run: n_cubes, n_strat, samples of the next fill, tile shape. */
+typedef struct {
+    int64_t n_eval_it, n_cubes, next_samples, max_tiles;
+    int32_t n_strat, n_intervals, n_dim, block, spt, grid, edges_smem, hist_smem;
+    double v_cubes;
+    int64_t fill_smem_bytes;
+} cvg_run_info;
+cvg_status cvg_run_info_get(cvg_run r, cvg_run_info *out);
+
+/* Backward: dI_it/dtheta of one iteration with that iteration's grid and nh
+ * (the current state of the run) held fixed and the same Philox samples as
+ * its fill (iteration counter `it`).  grad: host, n_params doubles. */
+cvg_status cvg_run_grad(cvg_run r, uint32_t it, double *grad);
+
+/* Compile the fill kernel (and the gradient kernel when has_grad) for
+ * `source` with NVRTC only -- no GPU needed -- for build checks.  `arch` such
+ * as "sm_103a"; `log` (may be NULL) receives the NVRTC log. */
+cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int32_t n_params,
+                             int32_t has_grad, int32_t precision, const char *arch, char *log,
+                             size_t log_len);
+
+/* Device timing of the last fill launch (CUDA events on the launch stream). */
+cvg_status cvg_run_last_fill_ms(cvg_run r, float *ms);
+/* Durations (ms) of the fill launches timed since the previous call
+ * (CVG_FLAG_TIME_FILL); synchronises.  At most `cap` values; *n = count. */
+cvg_status cvg_run_fill_times(cvg_run r, float *ms, int32_t cap, int32_t *n);
+
+/* Throughput microbenchmark of this device: kind 0 = FP32 FMA, 1 = FP64 FMA
+ * (TFLOP/s, 2 flops per FMA), 2 = device-memory copy (GB/s, read+write). */
+cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

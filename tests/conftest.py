@@ -1,0 +1,19 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); runs the CUDA path")
+
+
+@pytest.fixture(scope="session")
+def ctx():
+    from cuvegas_gb300 import _build, runtime
+    _build.build()
+    return runtime.default_context(0)

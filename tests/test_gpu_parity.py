@@ -1,0 +1,212 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the
+same inputs.  FP64 map arithmetic is identical by construction (same explicit
+fma sequence, same Philox words), so bin counts must match exactly and float
+sums to summation-order rounding."""
+import numpy as np
+import pytest
+
+from cuvegas_gb300 import _lib as L, integrands as I, runtime
+from oracle import analytic as A
+from oracle import pyoracle as P
+
+pytestmark = pytest.mark.gpu
+
+GAUSS_TH = np.array([0.5, 0.1])
+
+
+def make_run(ctx, src, dim, n_it, max_it, N=64, prec=L.PREC_FP64, seed=1, theta=None, P_=0,
+             grad=False, **kw):
+    f = ctx.integrand(src, dim, n_params=P_, has_grad=grad)
+    p = runtime.make_params(dim, n_it * max_it, max_it, n_intervals=N, seed=seed, precision=prec,
+                            **kw)
+    return runtime.Run(f, p, theta)
+
+
+def oracle_run(dim, n_it, max_it, N=64):
+    return P.OracleRun(dim, n_it * max_it, max_it, n_intervals=N)
+
+
+def relerr(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+
+
+@pytest.mark.parametrize("dim,n_it,N", [(3, 30000, 64), (1, 5000, 16), (5, 20000, 128),
+                                        (2, 999, 2)])
+def test_fill_fp64_matches_oracle(ctx, dim, n_it, N):
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=5) as r:
+        r.step(L.STAGE_FILL)
+        JF, JF2 = r.get(L.BUF_JF), r.get(L.BUF_JF2)
+        W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+    o = oracle_run(dim, n_it, 4, N)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=5)
+    S = o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    assert Cn.sum() == S * dim
+    assert np.array_equal(Cn.astype(np.int64), o.counts)
+    np.testing.assert_allclose(JF, o.JF, rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(JF2, o.JF2, rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(W, o.weights, rtol=1e-11, atol=1e-300)
+
+
+def test_fill_replay_uniforms_matches_oracle(ctx):
+    dim, n_it, N = 3, 20000, 32
+    o = oracle_run(dim, n_it, 2, N)
+    S = int(o.nh_sum[-1])
+    ub = np.random.default_rng(9).uniform(0, 1, size=(S, dim)).astype(np.float32)
+    ub[::97, 0] = 1.0                    # curand_uniform may return exactly 1
+    with make_run(ctx, I.GAUSS, dim, n_it, 2, N=N) as r:
+        r.set(L.BUF_UNIFORMS, ub)
+        r.step(L.STAGE_FILL)
+        JF, JF2 = r.get(L.BUF_JF), r.get(L.BUF_JF2)
+        W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+    u, keep = P.uniforms(P.U_BUFFER, ubuf=ub)
+    o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    assert np.array_equal(Cn.astype(np.int64), o.counts)
+    np.testing.assert_allclose(JF, o.JF, rtol=1e-12)
+    np.testing.assert_allclose(JF2, o.JF2, rtol=1e-12)
+    np.testing.assert_allclose(W, o.weights, rtol=1e-11)
+
+
+def test_realloc_matches_oracle(ctx):
+    dim, n_it, N = 3, 30000, 64
+    o = oracle_run(dim, n_it, 4, N)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=2)
+    o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=2) as r:
+        r.set(L.BUF_JF, o.JF)
+        r.set(L.BUF_JF2, o.JF2)
+        r.step(L.STAGE_REALLOC)
+        nh, dh = r.get(L.BUF_NH), r.get(L.BUF_DH)
+        nh_sum = r.get(L.BUF_NH_SUM)
+        res, it_res, it_sig = r.result()
+        assert r.get(L.BUF_ITERATION)[0] == 1
+        assert not r.get(L.BUF_JF).any()      # consumed and cleared
+    dsum, ri, si = o.results()
+    np.testing.assert_allclose(dh, o.dh, rtol=1e-13)
+    np.testing.assert_allclose([it_res[0], it_sig[0]], [ri, si], rtol=1e-12)
+    o.update_nh(dsum)
+    assert np.array_equal(nh.astype(np.int64), o.nh)
+    assert np.array_equal(nh_sum.astype(np.int64), o.nh_sum)
+
+
+def test_refine_matches_oracle(ctx):
+    dim, N = 4, 256
+    rng = np.random.default_rng(4)
+    w = rng.gamma(1.5, 2.0, size=(dim, N))
+    c = rng.integers(0, 40, size=(dim, N))
+    w[c == 0] = 0.0
+    o = oracle_run(dim, 50000, 3, N)
+    xe = o.x_edges
+    xe[:, 1:-1] = np.sort(rng.uniform(0, 1, size=(dim, N - 1)), axis=1)
+    o.set_x_edges(xe)
+    o.set_hist(w, c)
+    o.refine()
+    with make_run(ctx, I.GAUSS, dim, 50000, 3, N=N) as r:
+        r.set(L.BUF_X_EDGES, xe)
+        r.set(L.BUF_WEIGHTS, w)
+        r.set(L.BUF_COUNTS, c.astype(np.uint32))
+        r.step(L.STAGE_REFINE)
+        got = r.get(L.BUF_X_EDGES)
+        assert not r.get(L.BUF_WEIGHTS).any() and not r.get(L.BUF_COUNTS).any()
+    np.testing.assert_allclose(got, o.x_edges, rtol=1e-12, atol=1e-15)
+    assert np.all(np.diff(got, axis=1) > 0)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_full_run_fp64_matches_oracle(ctx, graph):
+    dim, n_it, max_it, N = 3, 40000, 6, 128
+    with make_run(ctx, I.GAUSS, dim, n_it, max_it, N=N, seed=3, skip=2,
+                  flags=L.FLAG_GRAPH if graph else 0) as r:
+        r.iterate(max_it)
+        res, it_res, it_sig = r.result()
+        xe = r.get(L.BUF_X_EDGES)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=3)
+    o = P.integrate(P.F_GAUSS, dim, n_it * max_it, max_it, theta=GAUSS_TH, skip=2,
+                    n_intervals=N, u=u)
+    assert res.tot_nevals == o["tot_nevals"]
+    assert relerr(it_res, o["it_res"]) < 1e-9
+    assert relerr(it_sig, o["it_sig"]) < 1e-8
+    assert abs(res.result - o["result"]) / abs(o["result"]) < 1e-10
+    assert abs(res.error - o["error"]) / o["error"] < 1e-8
+    np.testing.assert_allclose(xe, o["x_edges"], rtol=1e-9, atol=1e-12)
+
+
+def test_single_cube_and_fp32_against_fp64_oracle(ctx):
+    """n_strat = 1 (d=12, 1e4 evals/iteration): one hypercube holds every sample;
+    the reference maps this case on the CPU, here it stays on the GPU."""
+    dim, n_it, max_it = 12, 10000, 5
+    th = np.concatenate([np.full(dim, 8.0), np.full(dim, 0.4)])
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=8)
+    o = P.integrate(P.F_PRODPEAK, dim, n_it * max_it, max_it, theta=th, skip=1,
+                    n_intervals=64, u=u)
+    with make_run(ctx, I.PRODPEAK, dim, n_it, max_it, N=64, seed=8, theta=th, P_=2 * dim,
+                  skip=1) as r:
+        assert r.info.n_cubes == 1
+        r.iterate(max_it)
+        res, _, _ = r.result()
+    assert res.tot_nevals == o["tot_nevals"]
+    assert abs(res.result - o["result"]) / abs(o["result"]) < 1e-10
+    with make_run(ctx, I.PRODPEAK, dim, n_it, max_it, N=64, seed=8, theta=th, P_=2 * dim,
+                  skip=1, precision=L.PREC_FP32) as r:
+        r.iterate(max_it)
+        r32, _, _ = r.result()
+    assert abs(r32.result - o["result"]) < 0.2 * o["error"]
+
+
+def test_global_histogram_path(ctx):
+    """d=16 with 4096 bins in FP64 does not fit shared memory: grid and bin
+    sums go through global memory; results must not change."""
+    dim, n_it, N = 16, 200000, 4096
+    th = np.linspace(0.1, 1.0, dim)
+    with make_run(ctx, I.CORNER, dim, n_it, 2, N=N, seed=4, theta=th, P_=dim) as r:
+        assert r.info.hist_smem == 0
+        r.step(L.STAGE_FILL)
+        JF, Cn = r.get(L.BUF_JF), r.get(L.BUF_COUNTS)
+    o = oracle_run(dim, n_it, 2, N)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=4)
+    o.fill(P.F_CORNER, th, u, it=0)
+    assert np.array_equal(Cn.astype(np.int64), o.counts)
+    np.testing.assert_allclose(JF, o.JF, rtol=1e-12)
+
+
+def test_c1_fp64_and_fp32_against_analytic(ctx):
+    """C1 shape: d=4, 1e6 evals/iteration, 10 iterations, 1024 bins."""
+    exact = A.gauss_normalised(4)
+    out = {}
+    for prec in (L.PREC_FP64, L.PREC_FP32):
+        with make_run(ctx, I.GAUSS, 4, 1_000_000, 10, N=1024, seed=0, precision=prec,
+                      flags=L.FLAG_GRAPH) as r:
+            r.iterate(10)
+            res, _, _ = r.result()
+        out[prec] = res
+        assert abs(res.result - exact) < 4 * res.error, (prec, res.result, exact, res.error)
+        assert np.isfinite(res.chi2_dof)
+        assert res.error / exact < 1e-4
+    # same Philox stream: FP32 and FP64 estimates agree far inside the error
+    assert abs(out[0].result - out[1].result) < 0.5 * out[0].error
+
+
+def test_gradient_matches_oracle(ctx):
+    dim = 6
+    th = I.mixture_theta(0, dim)
+    with make_run(ctx, I.MIXTURE, dim, 50000, 3, N=128, seed=6, theta=th, P_=16,
+                  grad=True) as r:
+        r.step(L.STAGE_FILL | L.STAGE_REFINE | L.STAGE_REALLOC)   # adapt once
+        xe, nh = r.get(L.BUF_X_EDGES), r.get(L.BUF_NH)
+        g = r.grad()                       # iteration 1 samples, current grid/nh
+    o = oracle_run(dim, 50000, 3, 128)
+    o.set_x_edges(xe)
+    o.set_nh(nh.astype(np.int64))
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=6)
+    go = o.grad(P.F_MIXTURE, th, 16, u, it=1)
+    np.testing.assert_allclose(g, go, rtol=1e-9, atol=1e-14)
+
+
+def test_state_checks(ctx):
+    with make_run(ctx, I.GAUSS, 2, 1000, 2, N=16) as r:
+        with pytest.raises(L.CuvegasError):
+            r.set(L.BUF_NH, np.ones(r.info.n_cubes, dtype=np.uint32))   # nh < 2
+        r.iterate(2)
+        with pytest.raises(L.CuvegasError) as e:
+            r.iterate(1)
+        assert e.value.status == L.ERR_STATE
