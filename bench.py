@@ -370,9 +370,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline number only")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--evals", type=int, default=0,
+                    help="evals/iteration override (profiling runs on a smaller case)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.evals:
+        global N_IT
+        N_IT = args.evals
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -147,7 +147,7 @@ def test_single_cube_and_fp32_against_fp64_oracle(ctx):
     assert res.tot_nevals == o["tot_nevals"]
     assert abs(res.result - o["result"]) / abs(o["result"]) < 1e-10
     with make_run(ctx, I.PRODPEAK, dim, n_it, max_it, N=64, seed=8, theta=th, P_=2 * dim,
-                  skip=1, precision=L.PREC_FP32) as r:
+                  skip=1, prec=L.PREC_FP32) as r:
         r.iterate(max_it)
         r32, _, _ = r.result()
     assert abs(r32.result - o["result"]) < 0.2 * o["error"]
@@ -174,7 +174,7 @@ def test_c1_fp64_and_fp32_against_analytic(ctx):
     exact = A.gauss_normalised(4)
     out = {}
     for prec in (L.PREC_FP64, L.PREC_FP32):
-        with make_run(ctx, I.GAUSS, 4, 1_000_000, 10, N=1024, seed=0, precision=prec,
+        with make_run(ctx, I.GAUSS, 4, 1_000_000, 10, N=1024, seed=0, prec=prec,
                       flags=L.FLAG_GRAPH) as r:
             r.iterate(10)
             res, _, _ = r.result()
