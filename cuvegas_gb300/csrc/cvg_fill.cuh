@@ -13,10 +13,15 @@
 // tile_samples consecutive samples; thread t of a tile owns spt consecutive
 // samples, so a thread stays inside one cube for a run of samples and keeps
 // Sum f*jac and Sum (f*jac)^2 of that run in registers (compensated in FP32).
-// A run ends at a cube boundary or at the end of the thread's slice and is
-// added to JF/JF2 with one FP64 atomic each.  Per-bin Sum (f*jac)^2 and counts
-// go to shared-memory histograms, added to the global FP64/u32 histograms
-// once per CTA at the end.
+// A run that starts and ends inside the thread's slice covers its whole cube
+// and is stored; a run touching either end of the slice may be shared with a
+// neighbour and is added with an FP64 atomic.  Per-bin Sum (f*jac)^2 and
+// counts go to shared-memory histograms, added to the global FP64/u32
+// histograms once per CTA at the end.
+//
+// The FP32 form issues no FP64-pipe instruction per sample: bins are found
+// without float/int conversions and run sums are widened to FP64 by bit
+// splicing before the (L2-executed) FP64 atomics.
 //
 // Expects, before inclusion: cvg_common.cuh, and the macros
 //   CVG_F(x, th)          -> integrand value at x (T* x, const T* th)
@@ -32,34 +37,85 @@ template <> struct cvg_grid_src<double> {
     static CVG_D const double *get(const cvg_fill_args &a) { return a.x_edges; }
 };
 
-// Running sum of one cube run.  FP32: Kahan-compensated; FP64: plain.
+// Running sum.  FP32: Kahan-compensated; FP64: plain.
 template <typename T> struct cvg_acc;
 template <> struct cvg_acc<float> {
     float s, k;
     CVG_D void reset() { s = 0.f; k = 0.f; }
     CVG_D void add(float x) { const float y = x - k; const float t = s + y; k = (t - s) - y; s = t; }
     CVG_D double value() const { return (double)s - (double)k; }
+    CVG_D float value_t() const { return s - k; }
 };
 template <> struct cvg_acc<double> {
     double s;
     CVG_D void reset() { s = 0.0; }
     CVG_D void add(double x) { s += x; }
     CVG_D double value() const { return s; }
+    CVG_D double value_t() const { return s; }
 };
 
 CVG_D float cvg_fma(float a, float b, float c) { return fmaf(a, b, c); }
 CVG_D double cvg_fma(double a, double b, double c) { return fma(a, b, c); }
 
+// Exact float -> double by bit splicing (no FP64-pipe instruction); zero is
+// spliced too, denormals, inf and nan take the ordinary conversion.
+CVG_D double cvg_f2d(float f)
+{
+    const cvg_u32 u = __float_as_uint(f);
+    const cvg_u32 e = (u >> 23) & 0xFFu;
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (e == 0u || e == 0xFFu) return (double)f;
+    const cvg_u32 hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+CVG_D double cvg_to_double(float f) { return cvg_f2d(f); }
+CVG_D double cvg_to_double(double f) { return f; }
+
+// Bin of z = y*N (0 <= z <= N) and the fraction inside it:
+// b = min(floor(z), N-1), frac = z - b (src/main.cu:49-52).  The FP32 form
+// floors by a round-down add of 2^23 (no float/int conversion instruction).
+CVG_D int cvg_bin(float z, int N, float fNm1, float &frac)
+{
+    const float C = 8388608.0f;
+    const float bf = fminf(fmaxf(__fadd_rd(z, C) - C, 0.0f), fNm1);
+    frac = z - bf;
+    return __float_as_int(bf + C) - 0x4B000000;
+}
+CVG_D int cvg_bin(double z, int N, double, double &frac)
+{
+    int b = (int)z;
+    b = b < N - 1 ? b : N - 1;
+    b = b > 0 ? b : 0;
+    frac = z - (double)b;
+    return b;
+}
+
 // Stratum offsets coord_d * dy of cube c (digit d of c in base n_strat, least
-// significant first: src/main.cu:43-47).
+// significant first: src/main.cu:43-47); cvg_cube_next steps to cube c+1
+// like an odometer.
 template <int D, typename T>
-CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, T *cdy)
+CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, int *coord, T *cdy)
 {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const cvg_u32 q = c / ns;
-        cdy[d] = (T)(c - q * ns) * dy;
+        coord[d] = (int)(c - q * ns);
+        cdy[d] = (T)coord[d] * dy;
         c = q;
+    }
+}
+template <int D, typename T>
+CVG_D void cvg_cube_next(int ns, T dy, int *coord, T *cdy)
+{
+    bool carry = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        if (carry) {
+            const int v = coord[d] + 1;
+            carry = v == ns;
+            coord[d] = carry ? 0 : v;
+            cdy[d] = (T)coord[d] * dy;
+        }
     }
 }
 
@@ -106,14 +162,16 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     const cvg_u32 it = *a.iteration;
     const cvg_u32 k0 = (cvg_u32)a.seed, k1 = (cvg_u32)(a.seed >> 32);
     const cvg_u32 c3 = a.instance << 8;
-    const cvg_u32 ns = (cvg_u32)a.n_strat;
-    const T dy = (T)1 / (T)a.n_strat;
+    const int ns = a.n_strat;
+    const T dy = (T)1 / (T)ns;
     const T fN = (T)N;
+    const T fNm1 = (T)(N - 1);
     const T *G = ESM ? E : grid;
+    const T vc = (T)a.v_cubes;
 
-    double gtot[PP];
+    cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
 #pragma unroll
-    for (int p = 0; p < PP; ++p) gtot[p] = 0.0;
+    for (int p = 0; p < PP; ++p) gacc[p].reset();
 
     __syncthreads();
 
@@ -142,10 +200,12 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
             }
             int ci = lo;
             cvg_u32 c = c_lo + (cvg_u32)ci;
+            int cstart = starts[ci];
             int next = starts[ci + 1];
-            cvg_u32 j = (cvg_u32)(l0 - starts[ci]);
+            cvg_u32 j = (cvg_u32)(l0 - cstart);
+            int coord[D];
             T cdy[D];
-            cvg_cube_offsets<D, T>(c, ns, dy, cdy);
+            cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
             const int lend = min(l0 + spt, lend_tile);
 
             cvg_acc<T> a1, a2;
@@ -153,28 +213,33 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
             T ag[PP];
 #pragma unroll
             for (int p = 0; p < PP; ++p) ag[p] = (T)0;
-            int run = 0;  // samples in the current cube run
+            int run = 0;   // samples in the current cube run
 
             for (int l = l0; l < lend; ++l) {
                 if (l >= next) {
+                    // run [max(cstart, l0), next) is complete: private to this
+                    // thread unless its cube began before l0
                     if (run > 0) {
                         if (GRAD) {
-                            const double sc = a.v_cubes / (double)(next - starts[ci]);
+                            const T sc = vc / (T)(next - cstart);
 #pragma unroll
-                            for (int p = 0; p < PP; ++p) { gtot[p] += (double)ag[p] * sc; ag[p] = (T)0; }
+                            for (int p = 0; p < PP; ++p) { gacc[p].add(ag[p] * sc); ag[p] = (T)0; }
                         } else {
-                            atomicAdd(&a.JF[c], a1.value());
-                            atomicAdd(&a.JF2[c], a2.value());
+                            const double v1 = cvg_to_double(a1.value_t());
+                            const double v2 = cvg_to_double(a2.value_t());
+                            if (cstart >= l0) { a.JF[c] = v1; a.JF2[c] = v2; }
+                            else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
                             a1.reset(); a2.reset();
                         }
                         run = 0;
                     }
                     do {  // empty cubes (never produced by the reallocation) are skipped
                         ++ci; ++c;
+                        cvg_cube_next<D, T>(ns, dy, coord, cdy);
+                        cstart = next;
                         next = starts[ci + 1];
                     } while (l >= next && ci < K - 2);
                     j = 0u;
-                    cvg_cube_offsets<D, T>(c, ns, dy, cdy);
                 }
                 ++run;
                 cvg_u32 rr[NB * 4];
@@ -196,13 +261,12 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
                     else u = cvg_uniform<T>(rr[d]);
                     const T y = cvg_fma(u, dy, cdy[d]);
                     const T z = y * fN;
-                    int b = (int)z;
-                    b = b < N - 1 ? b : N - 1;
-                    b = b > 0 ? b : 0;
+                    T frac;
+                    const int b = cvg_bin(z, N, fNm1, frac);
                     const T e0 = G[d * (N + 1) + b];
                     const T e1 = G[d * (N + 1) + b + 1];
                     const T dx = e1 - e0;
-                    x[d] = cvg_fma(dx, z - (T)b, e0);
+                    x[d] = cvg_fma(dx, frac, e0);
                     jac *= fN * dx;
                     bin[d] = b;
                 }
@@ -222,7 +286,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
                             atomicAdd(&hw[d * N + bin[d]], jf2);
                             atomicAdd(&hc[d * N + bin[d]], 1u);
                         } else {
-                            atomicAdd(&a.weights[d * N + bin[d]], (double)jf2);
+                            atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
                             atomicAdd(&a.counts[d * N + bin[d]], 1u);
                         }
                     }
@@ -231,14 +295,16 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
                 }
                 ++j;
             }
-            if (run > 0) {
+            if (run > 0) {   // last run: private only if it began here and its cube ends here
                 if (GRAD) {
-                    const double sc = a.v_cubes / (double)(starts[ci + 1] - starts[ci]);
+                    const T sc = vc / (T)(next - cstart);
 #pragma unroll
-                    for (int p = 0; p < PP; ++p) gtot[p] += (double)ag[p] * sc;
+                    for (int p = 0; p < PP; ++p) gacc[p].add(ag[p] * sc);
                 } else {
-                    atomicAdd(&a.JF[c], a1.value());
-                    atomicAdd(&a.JF2[c], a2.value());
+                    const double v1 = cvg_to_double(a1.value_t());
+                    const double v2 = cvg_to_double(a2.value_t());
+                    if (cstart >= l0 && next == lend) { a.JF[c] = v1; a.JF2[c] = v2; }
+                    else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
                 }
             }
         }
@@ -250,7 +316,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
         for (int i = tid; i < D * N; i += BS) {
             const cvg_u32 cn = hc[i];
             if (cn) {
-                atomicAdd(&a.weights[i], (double)hw[i]);
+                atomicAdd(&a.weights[i], cvg_to_double(hw[i]));
                 atomicAdd(&a.counts[i], cn);
             }
         }
@@ -259,7 +325,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
         const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
         for (int p = 0; p < PP; ++p) {
-            double v = gtot[p];
+            double v = gacc[p].value();
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
             if (lane == 0) red[warp * PP + p] = v;

@@ -578,7 +578,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     const int64_t nh0 = std::max<int64_t>(2, (int64_t)(1.0 / (double)r->n_cubes * (double)r->n_eval_it));
 
     // tile shape
-    r->block = p.block > 0 ? p.block : 256;
+    r->block = p.block > 0 ? p.block : 512;
     r->spt = p.spt > 0 ? p.spt : 8;
     if (r->block % 32 || r->block > 1024) { delete r; return fail(CVG_ERR_INVALID, "block must be a multiple of 32, <= 1024"); }
     if (r->spt < 1 || r->spt > 256) { delete r; return fail(CVG_ERR_INVALID, "spt must be in [1, 256]"); }

@@ -11,6 +11,9 @@
 // 667-694) and the histogram reset (src/main.cu:147-158).
 #include "cvg_kernels.cuh"
 
+#include <cooperative_groups.h>
+namespace cg = cooperative_groups;
+
 namespace {
 
 constexpr int RB = 256;                       // reallocation block
@@ -68,21 +71,57 @@ __device__ __forceinline__ cvg_u64 block_exscan_u64(cvg_u64 &v, cvg_u64 *scratch
     return total;
 }
 
-// d^beta for d > 0 through FP32 log2/exp2 with the binary exponent kept exact
-// (relative error ~1e-6; used for the FP32 form's allocation only).
-__device__ __forceinline__ double fast_pow_pos(double t, double beta)
+// ---- FP32-form helpers: no FP64-pipe instruction per hypercube ----
+
+// float -> double by bit splicing (zero, denormals, inf, nan converted normally)
+__device__ __forceinline__ double f2d_bits(float f)
 {
-    if (!(t > 0.0)) return 0.0;
-    if (!(t < 1.0e300)) return pow(t, beta);
-    int scale = 0;
-    if (t < 1.0e-290) { t *= 18446744073709551616.0; scale = -64; }   // 2^64
-    const int hi = __double2hiint(t), lo = __double2loint(t);
-    const int e = ((hi >> 20) & 0x7ff) - 1023 + scale;
-    const float m = __int_as_float(0x3F800000 | ((hi & 0xFFFFF) << 3) | ((unsigned)lo >> 29));
-    const double y = beta * (double)e + (double)((float)beta * log2f(m));
-    const double k = floor(y);
-    const float f = exp2f((float)(y - k));           // in [1, 2)
-    return ldexp((double)f, (int)k);
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (e == 0u || e == 0xFFu) return (double)f;
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)),
+                            (int)(u << 29));
+}
+
+// double -> (hi, lo) floats holding the top 48 significand bits, integer ops
+// only; values outside the float range take the ordinary conversion.
+__device__ __forceinline__ void df_split(double x, float &hi, float &lo)
+{
+    const int h = __double2hiint(x);
+    const unsigned l = (unsigned)__double2loint(x);
+    const unsigned sign = (unsigned)h & 0x80000000u;
+    const int e = ((h >> 20) & 0x7FF) - 1023;
+    if (((h & 0x7FFFFFFF) | (int)l) == 0) { hi = 0.f; lo = 0.f; return; }
+    if (e < -125 || e > 127) { hi = (float)x; lo = 0.f; return; }
+    hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (((unsigned)h & 0xFFFFFu) << 3) |
+                         (l >> 29));
+    const unsigned rem = l & 0x1FFFFFFFu;
+    if (rem == 0u || e < -74) { lo = 0.f; return; }
+    const float sc = __uint_as_float((unsigned)(e + 75) << 23);   // 2^(e-52)
+    lo = __uint_as_float(sign | __float_as_uint((float)rem * sc));
+}
+
+// double -> float (truncation), integer ops only
+__device__ __forceinline__ float d2f_bits(double x)
+{
+    float hi, lo;
+    df_split(x, hi, lo);
+    return hi;
+}
+
+struct dfloat { float h, l; };
+
+__device__ __forceinline__ dfloat df_add(dfloat a, dfloat b)
+{
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float err = (a.h - (s - bb)) + (b.h - bb);
+    const float t = err + a.l + b.l;
+    dfloat r;
+    r.h = s + t;
+    r.l = t - (r.h - s);
+    return r;
 }
 
 __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
@@ -98,27 +137,15 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
         const double jf = a.JF[c], jf2 = a.JF2[c];
         a.JF[c] = 0.0;
         a.JF2[c] = 0.0;
-        double dh;
-        if (!a.fast_pow) {
-            // src/main.cu:88-102, same operation order
-            const double Ih = jf / neval * vc;
-            const double Sig2 = (jf2 / neval * vc * vc) - (Ih * Ih);
-            v[1] += Ih;
-            v[2] += Sig2 / neval;
-            const double m = vc * jf / neval;
-            double t = vc * vc * jf2 / neval - m * m;
-            if (t < 0) t = 0;
-            dh = pow(t, a.beta);
-        } else {
-            const double inv = 1.0 / (double)neval;
-            const double Ih = jf * inv * vc;
-            const double Sig2 = jf2 * inv * vc * vc - Ih * Ih;
-            v[1] += Ih;
-            v[2] += Sig2 * inv;
-            double t = Sig2;
-            if (t < 0) t = 0;
-            dh = fast_pow_pos(t, a.beta);
-        }
+        // src/main.cu:88-102, same operation order
+        const double Ih = jf / neval * vc;
+        const double Sig2 = (jf2 / neval * vc * vc) - (Ih * Ih);
+        v[1] += Ih;
+        v[2] += Sig2 / neval;
+        const double m = vc * jf / neval;
+        double t = vc * vc * jf2 / neval - m * m;
+        if (t < 0) t = 0;
+        const double dh = pow(t, a.beta);
         a.dh[c] = dh;
         v[0] += dh;
     }
@@ -127,6 +154,77 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
         a.partials[3 * blockIdx.x + 0] = v[0];
         a.partials[3 * blockIdx.x + 1] = v[1];
         a.partials[3 * blockIdx.x + 2] = v[2];
+    }
+}
+
+// FP32 form of k3_results.  Per cube, with m = JF/n and q = JF2/n held as
+// double-floats (48-bit significands): I_h / V = m, sigma2_h / V^2 = q - m^2,
+// d_h = (q - m^2)^beta (the constant V^(2 beta) cancels in the allocation).
+// Sums are compensated in FP32 per thread, FP64 across warps and blocks;
+// k3_finish multiplies by V and V^2.
+__global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
+{
+    __shared__ double wsum[3][RB / 32];
+    const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
+    const float beta = (float)a.beta;
+    dfloat sm = {0.f, 0.f};
+    float sv = 0.f, kv = 0.f, sd = 0.f, kd = 0.f;   // Kahan sums of var/n and d_h
+    for (int k = 0; k < RIPT; ++k) {
+        const cvg_u32 c = base + k * RB + threadIdx.x;
+        if (c >= a.n_cubes) break;
+        const int neval = (int)(a.nh_sum[c + 1] - a.nh_sum[c]);
+        float jh, jl, qh, ql;
+        df_split(a.JF[c], jh, jl);
+        df_split(a.JF2[c], qh, ql);
+        a.JF[c] = 0.0;
+        a.JF2[c] = 0.0;
+        const float fn = (float)neval;
+        const float inv = 1.0f / fn;
+        // m = JF/n, q = JF2/n as double-floats
+        float mh = jh * inv;
+        float ml = (fmaf(-mh, fn, jh) + jl) * inv;
+        float qq = qh * inv;
+        float qlo = (fmaf(-qq, fn, qh) + ql) * inv;
+        // var = q - m^2 (the leading difference is exact when it cancels)
+        const float p = mh * mh;
+        const float pe = fmaf(mh, mh, -p) + 2.0f * mh * ml;
+        float var = (qq - p) + (qlo - pe);
+        var = var > 0.f ? var : 0.f;
+        dfloat mv = {mh, ml};
+        sm = df_add(sm, mv);
+        {
+            const float y = var * inv - kv, t = sv + y;
+            kv = (t - sv) - y; sv = t;
+        }
+        const float dh = var > 0.f ? exp2f(beta * log2f(var)) : 0.f;
+        {
+            const float y = dh - kd, t = sd + y;
+            kd = (t - sd) - y; sd = t;
+        }
+        a.dh[c] = f2d_bits(dh);
+    }
+    // warp reduction in FP32 (double-float for the estimate)
+    float v = sv - kv, d = sd - kd;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        dfloat other = {__shfl_down_sync(0xffffffffu, sm.h, o), __shfl_down_sync(0xffffffffu, sm.l, o)};
+        sm = df_add(sm, other);
+        v += __shfl_down_sync(0xffffffffu, v, o);
+        d += __shfl_down_sync(0xffffffffu, d, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        wsum[0][warp] = f2d_bits(d);
+        wsum[1][warp] = f2d_bits(sm.h) + f2d_bits(sm.l);
+        wsum[2][warp] = f2d_bits(v);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+        for (int w = 0; w < RB / 32; ++w) { t0 += wsum[0][w]; t1 += wsum[1][w]; t2 += wsum[2][w]; }
+        a.partials[3 * blockIdx.x + 0] = t0;
+        a.partials[3 * blockIdx.x + 1] = t1;
+        a.partials[3 * blockIdx.x + 2] = t2;
     }
 }
 
@@ -142,7 +240,11 @@ __global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned n
     block_sum<3>(v, scratch);
     if (threadIdx.x == 0) {
         const cvg_u32 it = *a.iteration;
-        const double r = v[1], s = v[2];
+        double r = v[1], s = v[2];
+        if (a.fast_pow) {   // FP32 form sums m and var/n without the cube volume
+            r *= a.v_cubes;
+            s *= a.v_cubes * a.v_cubes;
+        }
         if ((int)it < a.max_it) {
             a.stats[it] = r;
             a.stats[a.max_it + it] = s;
@@ -150,6 +252,7 @@ __global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned n
         }
         cvg_acc_dev *acc = a.acc;
         acc->dh_sum = v[0];
+        acc->nh_scale = (double)a.n_eval_it / v[0];
         const cvg_u64 S = a.nh_sum[a.n_cubes];
         acc->tot_nevals += S;
         acc->last_nevals = S;
@@ -166,13 +269,16 @@ __global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned n
 
 // mode 0: nh from the damped variances (updateNh, src/main.cu:173-187)
 // mode 1: nh_new already holds the counts (initialisation / state import)
+// mode 2: FP32 form, nh = floor(d_h * n_eval_it / sum d_h) in FP32
 __global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
 {
-    __shared__ double scratch[32];
+    __shared__ cvg_u64 wtot[RB / 32];
     const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
-    const double dsum = a.acc->dh_sum;
-    const double n_it = (double)a.n_eval_it;
-    double tot = 0.0;   // counts are exact in double (< 2^53)
+    double dsum = 0.0, n_it = 0.0;
+    float scale = 0.f;
+    if (mode == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
+    if (mode == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;   // round the total down
+    cvg_u64 tot = 0;
     for (int k = 0; k < RIPT; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
@@ -184,14 +290,25 @@ __global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
             int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
             nh = ns < 2 ? 2u : (cvg_u32)ns;
             a.nh_new[c] = nh;
+        } else if (mode == 2) {
+            const float x = d2f_bits(a.dh[c]) * scale;
+            const int ns = (x >= 0.f && x < 2147483520.f) ? (int)x : (x >= 2147483520.f ? 2147483520 : 0);
+            nh = ns < 2 ? 2u : (cvg_u32)ns;
+            a.nh_new[c] = nh;
         } else {
             nh = a.nh_new[c];
         }
-        tot += (double)nh;
+        tot += nh;
     }
-    double v[1] = {tot};
-    block_sum<1>(v, scratch);
-    if (threadIdx.x == 0) a.bsums[blockIdx.x] = (cvg_u64)v[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+    if ((threadIdx.x & 31) == 0) wtot[threadIdx.x >> 5] = tot;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        cvg_u64 t = 0;
+        for (int w = 0; w < RB / 32; ++w) t += wtot[w];
+        a.bsums[blockIdx.x] = t;
+    }
 }
 
 __global__ void __launch_bounds__(1024) k3_scan(cvg_realloc_args a, unsigned nb)
@@ -244,98 +361,147 @@ __global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb)
 }
 
 // ---------------------------------------------------------------------------
-// K4: grid refinement, one CTA per dimension, FP64.
+// K4: grid refinement, FP64.  One thread-block cluster of CL CTAs per
+// dimension: CTA r owns bins [r*B, (r+1)*B).  Partial sums and scan offsets
+// are exchanged through distributed shared memory, so the FP64 pow/log of
+// the damping run on CL SMs per dimension instead of one.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(CVG_REFINE_BLOCK) k4_refine(cvg_refine_args a)
+constexpr int CL = 8;      // CTAs per cluster (portable size)
+constexpr int KB = 128;    // threads per CTA
+
+__device__ __forceinline__ double cl_sum(cg::cluster_group &cl, double *slot)
+{
+    double t = 0.0;
+    for (int q = 0; q < CL; ++q) t += *cl.map_shared_rank(slot, q);   // same order everywhere
+    return t;
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine(cvg_refine_args a)
 {
     extern __shared__ __align__(16) double ks[];
-    __shared__ double scratch[32];
-    const int N = a.n_intervals, d = blockIdx.x, tid = threadIdx.x, bs = blockDim.x;
-    double *w = ks, *sw = ks + N, *cs = ks + 2 * N, *xo = ks + 3 * N;
-    int *dv = (int *)(xo + N + 1);
+    __shared__ double part[4];
+    __shared__ double wscr[KB / 32];
+    cg::cluster_group cl = cg::this_cluster();
+    const int r = (int)cl.block_rank();
+    const int d = blockIdx.x / CL;
+    const int N = a.n_intervals, tid = threadIdx.x;
+    const int B = (N + CL - 1) / CL;
+    const int i0 = min(N, r * B), i1 = min(N, i0 + B), nb = i1 - i0;
+    // smem: w[B+2] (with halo) | sw[B] | cs[B] | fsw[N] | fcs[N] | xo[N+1] | fdv[N] (int)
+    double *w = ks, *sw = w + B + 2, *cs = sw + B, *fsw = cs + B, *fcs = fsw + N, *xo = fcs + N;
+    int *fdv = (int *)(xo + N + 1);
     double *xe = a.x_edges + (size_t)d * (N + 1);
     float *xe32 = a.x_edges32 + (size_t)d * (N + 1);
 
-    // normalizeWeights (src/main.cu:106-118) + resetWeights (147-158)
-    double part = 0.0;
-    for (int i = tid; i < N; i += bs) {
+    auto block_total = [&](double v) -> double {   // fixed-order block sum
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) wscr[tid >> 5] = v;
+        __syncthreads();
+        double t = 0.0;
+        for (int q = 0; q < KB / 32; ++q) t += wscr[q];
+        __syncthreads();
+        return t;
+    };
+
+    // normalizeWeights (src/main.cu:106-118) for own bins and one halo bin
+    // each side; the old grid row is kept in shared memory.
+    double p1 = 0.0;
+    for (int i = i0 - 1 + tid; i <= i1; i += KB) {
+        if (i < 0 || i >= N) continue;
         const size_t g = (size_t)d * N + i;
         const double wi = a.weights[g];
         const cvg_u32 cn = a.counts[g];
         const double x = cn != 0u ? wi / (double)cn : wi;
-        w[i] = x;
-        part += x;
-        a.weights[g] = 0.0;
-        a.counts[g] = 0u;
+        w[i - i0 + 1] = x;
+        if (i >= i0 && i < i1) p1 += x;
     }
-    for (int i = tid; i <= N; i += bs) xo[i] = xe[i];
-    double v[1] = {part};
-    block_sum<1>(v, scratch);          // d_sum (src/main.cu:668-670)
-    const double dsum = v[0];
+    for (int i = tid; i <= N; i += KB) xo[i] = xe[i];
+    p1 = block_total(p1);
+    if (tid == 0) part[0] = p1;
+    cl.sync();
+    const double dsum = cl_sum(cl, &part[0]);          // d_sum (src/main.cu:668-670)
+    for (int i = i0 + tid; i < i1; i += KB) {          // resetWeights (src/main.cu:147-158)
+        a.weights[(size_t)d * N + i] = 0.0;
+        a.counts[(size_t)d * N + i] = 0u;
+    }
     bool ok = a.adapt && dsum > 0.0 && isfinite(dsum);
 
     if (ok) {
         // smoothWeights (src/main.cu:120-145)
         double p2 = 0.0;
-        for (int i = tid; i < N; i += bs) {
+        for (int i = i0 + tid; i < i1; i += KB) {
+            const double wm = i > 0 ? w[i - i0] : 0.0, wc = w[i - i0 + 1];
+            const double wp = i < N - 1 ? w[i - i0 + 2] : 0.0;
             double t;
-            if (i == 0) t = (7.0 * w[0] + w[1]) / (8.0 * dsum);
-            else if (i == N - 1) t = (w[i - 1] + 7.0 * w[i]) / (8.0 * dsum);
-            else t = (w[i - 1] + 6.0 * w[i] + w[i + 1]) / (8.0 * dsum);
+            if (i == 0) t = (7.0 * wc + wp) / (8.0 * dsum);
+            else if (i == N - 1) t = (wm + 7.0 * wc) / (8.0 * dsum);
+            else t = (wm + 6.0 * wc + wp) / (8.0 * dsum);
             if (t != 0) t = pow((t - 1.0) / log(t), a.alpha);
-            sw[i] = t;
+            sw[i - i0] = t;
             p2 += t;
         }
-        v[0] = p2;
-        block_sum<1>(v, scratch);      // summed_weights (src/main.cu:673-675)
-        const double ssum = v[0];
-        ok = ssum > 0.0 && isfinite(ssum);
-        if (ok) {
-            // inclusive scan (src/main.cu:688-690): each thread a contiguous run
-            const int per = (N + bs - 1) / bs;
-            const int i0 = tid * per;
-            double loc = 0.0;
-            for (int k = 0; k < per && i0 + k < N; ++k) loc += sw[i0 + k];
-            // exclusive scan of the per-thread totals (doubles)
-            const int lane = tid & 31, warp = tid >> 5, nw = bs >> 5;
-            double x = loc;
+        __syncthreads();
+        // inclusive scan of own bins: each thread a contiguous run
+        const int per = (nb + KB - 1) / KB;
+        const int j0 = tid * per;
+        double loc = 0.0;
+        for (int k = 0; k < per && j0 + k < nb; ++k) loc += sw[j0 + k];
+        double x = loc;
+        const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const double y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wscr[warp] = x;
+        __syncthreads();
+        double woff = 0.0;
+        for (int q = 0; q < warp; ++q) woff += wscr[q];
+        double run = x - loc + woff;
+        for (int k = 0; k < per && j0 + k < nb; ++k) { run += sw[j0 + k]; cs[j0 + k] = run; }
+        __syncthreads();
+        p2 = block_total(p2);
+        if (tid == 0) { part[1] = p2; part[2] = nb > 0 ? cs[nb - 1] : 0.0; }
+        cl.sync();
+        const double ssum = cl_sum(cl, &part[1]);      // summed_weights (src/main.cu:673-675)
+        double pre = 0.0;
+        for (int q = 0; q < r; ++q) pre += *cl.map_shared_rank(&part[2], q);
+        ok = ssum > 0.0 && isfinite(ssum);
+        for (int j = tid; j < nb; j += KB) cs[j] += pre;
+        cl.sync();
+        if (ok) {
+            // gather sw and the scan of every bin of this dimension
+            for (int q = 0; q < CL; ++q) {
+                const int q0 = min(N, q * B), q1 = min(N, q0 + B);
+                const double *rsw = cl.map_shared_rank(sw, q), *rcs = cl.map_shared_rank(cs, q);
+                for (int j = tid; j < q1 - q0; j += KB) { fsw[q0 + j] = rsw[j]; fcs[q0 + j] = rcs[j]; }
             }
-            if (lane == 31) scratch[warp] = x;
-            __syncthreads();
-            if (tid == 0) {
-                double s = 0.0;
-                for (int q = 0; q < nw; ++q) { const double t = scratch[q]; scratch[q] = s; s += t; }
-            }
-            __syncthreads();
-            double run = x - loc + scratch[warp];
-            for (int k = 0; k < per && i0 + k < N; ++k) { run += sw[i0 + k]; cs[i0 + k] = run; }
             __syncthreads();
             const double delta = ssum / N;
-            for (int i = tid; i < N; i += bs) dv[i] = (int)(cs[i] / delta);   // setMap div
+            for (int i = tid; i < N; i += KB) fdv[i] = (int)(fcs[i] / delta);   // setMap div
             __syncthreads();
-            // updateXEdges (src/main.cu:211-230): new edge k+1 lies in the old
-            // interval o = min{ i : div_i > k }, the interval setMap assigns to k.
-            for (int k = tid; k < N - 1; k += bs) {
+            // updateXEdges (src/main.cu:211-230): new edge k+1 lies in old
+            // interval o = min{ i : div_i > k }, the interval setMap assigns to k
+            for (int k = i0 + tid; k < min(i1, N - 1); k += KB) {
                 int lo = 0, hi = N - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi) >> 1;
-                    if (dv[mid] > k) hi = mid; else lo = mid + 1;
+                    if (fdv[mid] > k) hi = mid; else lo = mid + 1;
                 }
                 const int o = lo;
-                const double acc = (k + 1) * delta - (o > 0 ? cs[o - 1] : 0.0);
-                const double xn = fma(acc / sw[o], xo[o + 1] - xo[o], xo[o]);
+                const double acc = (k + 1) * delta - (o > 0 ? fcs[o - 1] : 0.0);
+                const double xn = fma(acc / fsw[o], xo[o + 1] - xo[o], xo[o]);
                 xe[k + 1] = xn;
                 xe32[k + 1] = (float)xn;
             }
+            if (r == 0 && tid == 0) xe32[0] = (float)xo[0];
+            if (i1 == N && i0 < N && tid == 0) xe32[N] = (float)xo[N];
         }
     }
-    if (!ok)
-        for (int i = tid; i <= N; i += bs) xe32[i] = (float)xo[i];
-    else if (tid == 0) { xe32[0] = (float)xo[0]; xe32[N] = (float)xo[N]; }
+    if (!ok && nb > 0)
+        for (int i = i0 + tid; i <= (i1 == N ? N : i1 - 1); i += KB) xe32[i] = (float)xo[i];
+    cl.sync();   // keep shared memory alive until every CTA has read it
 }
 
 __global__ void grid32(const double *x, float *x32, int n)
@@ -394,10 +560,11 @@ cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cuda
 cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s)
 {
     const unsigned nb = cvg_realloc_blocks(a.n_cubes);
-    k3_results<<<nb, RB, 0, s>>>(a);
+    if (a.fast_pow) k3_results_f32<<<nb, RB, 0, s>>>(a);
+    else k3_results<<<nb, RB, 0, s>>>(a);
     k3_finish<<<1, 1024, 0, s>>>(a, nb);
     if (a.adapt) {
-        k3_count<<<nb, RB, 0, s>>>(a, 0);
+        k3_count<<<nb, RB, 0, s>>>(a, a.fast_pow ? 2 : 0);
         k3_scan<<<1, 1024, 0, s>>>(a, nb);
         k3_apply<<<nb, RB, 0, s>>>(a, nb);
     }
@@ -420,14 +587,15 @@ cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cuda
 
 cudaError_t cvg_launch_refine(const cvg_refine_args &a, cudaStream_t s)
 {
-    const size_t smem = sizeof(double) * (4 * (size_t)a.n_intervals + 1) +
-                        sizeof(int) * (size_t)a.n_intervals + 16;
+    const int N = a.n_intervals, B = (N + CL - 1) / CL;
+    const size_t smem = sizeof(double) * ((size_t)(B + 2) + 2 * B + 2 * (size_t)N + N + 1) +
+                        sizeof(int) * (size_t)N + 16;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k4_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k4_refine<<<a.dim, CVG_REFINE_BLOCK, smem, s>>>(a);
+    k4_refine<<<a.dim * CL, KB, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -16,10 +16,10 @@ struct cvg_acc_dev {
     double swr;       // sum I/sigma2
     double swr2;      // sum I^2/sigma2
     double dh_sum;    // sum of damped cube variances of the last iteration
+    double nh_scale;  // n_eval_it / dh_sum (FP32 form's reallocation)
     cvg_u64 used;     // iterations in the mean
     cvg_u64 tot_nevals;
     cvg_u64 last_nevals;
-    cvg_u64 pad;
 };
 
 struct cvg_realloc_args {
@@ -42,7 +42,8 @@ struct cvg_realloc_args {
     int tile_samples;
     int skip;
     int max_it;
-    int fast_pow;           // 1: d_h^beta through FP32 log2/exp2 (FP32 form)
+    int fast_pow;           // 1: FP32 form (compensated FP32 per cube, FP64 sums); d_h is
+                            //    then (var)^beta without the cube-volume factor V^(2 beta)
     int adapt;              // 0: keep nh (no reallocation), still accumulate results
 };
 

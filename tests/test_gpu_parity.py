@@ -89,6 +89,27 @@ def test_realloc_matches_oracle(ctx):
     assert np.array_equal(nh_sum.astype(np.int64), o.nh_sum)
 
 
+def test_realloc_fp32_form_against_fp64_oracle(ctx):
+    """FP32 form: per-cube mean/variance in compensated FP32, sums in FP64.
+    Iteration estimate to 1e-10, variance to 1e-6, allocation within 1e-5."""
+    dim, n_it, N = 4, 200000, 64
+    o = oracle_run(dim, n_it, 4, N)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=12)
+    o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=12, prec=L.PREC_FP32) as r:
+        r.set(L.BUF_JF, o.JF)
+        r.set(L.BUF_JF2, o.JF2)
+        r.step(L.STAGE_REALLOC)
+        nh = r.get(L.BUF_NH).astype(np.int64)
+        st = r.get(L.BUF_STATS)
+    dsum, ri, si = o.results()
+    assert abs(st[0, 0] - ri) <= 1e-10 * abs(ri)
+    assert abs(st[1, 0] - si) <= 1e-6 * abs(si)
+    o.update_nh(dsum)
+    assert np.all(np.abs(nh - o.nh) <= 1 + 1e-5 * o.nh)
+    assert nh.sum() <= o.sz.n_eval_it + 2 * o.sz.n_cubes
+
+
 def test_refine_matches_oracle(ctx):
     dim, N = 4, 256
     rng = np.random.default_rng(4)
