@@ -142,8 +142,7 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
         const double Sig2 = (jf2 / neval * vc * vc) - (Ih * Ih);
         v[1] += Ih;
         v[2] += Sig2 / neval;
-        const double m = vc * jf / neval;
-        double t = vc * vc * jf2 / neval - m * m;
+        double t = vc * vc * jf2 / neval - pow(vc * jf / neval, 2);
         if (t < 0) t = 0;
         const double dh = pow(t, a.beta);
         a.dh[c] = dh;
