@@ -82,7 +82,8 @@ def test_realloc_matches_oracle(ctx):
         assert r.get(L.BUF_ITERATION)[0] == 1
         assert not r.get(L.BUF_JF).any()      # consumed and cleared
     dsum, ri, si = o.results()
-    np.testing.assert_allclose(dh, o.dh, rtol=1e-13)
+    # dh cancels; CUDA's and glibc's pow differ by an ulp, lifted to ~1e-13..1e-10
+    np.testing.assert_allclose(dh, o.dh, rtol=1e-9)
     np.testing.assert_allclose([it_res[0], it_sig[0]], [ri, si], rtol=1e-12)
     o.update_nh(dsum)
     assert np.array_equal(nh.astype(np.int64), o.nh)
