@@ -57,15 +57,16 @@ template <> struct cvg_acc<double> {
 CVG_D float cvg_fma(float a, float b, float c) { return fmaf(a, b, c); }
 CVG_D double cvg_fma(double a, double b, double c) { return fma(a, b, c); }
 
-// Exact float -> double by bit splicing (no FP64-pipe instruction); zero is
-// spliced too, denormals, inf and nan take the ordinary conversion.
+// float -> double by bit splicing (no FP64-pipe instruction): exact for
+// normal numbers; zero and denormals give signed zero, inf/nan stay inf/nan.
 CVG_D double cvg_f2d(float f)
 {
     const cvg_u32 u = __float_as_uint(f);
     const cvg_u32 e = (u >> 23) & 0xFFu;
-    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (e == 0u || e == 0xFFu) return (double)f;
-    const cvg_u32 hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const cvg_u32 sign = u & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    if (e == 0xFFu) return __hiloint2double((int)(sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3)), 0);
+    const cvg_u32 hi = sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
     return __hiloint2double((int)hi, (int)(u << 29));
 }
 CVG_D double cvg_to_double(float f) { return cvg_f2d(f); }

@@ -73,27 +73,30 @@ __device__ __forceinline__ cvg_u64 block_exscan_u64(cvg_u64 &v, cvg_u64 *scratch
 
 // ---- FP32-form helpers: no FP64-pipe instruction per hypercube ----
 
-// float -> double by bit splicing (zero, denormals, inf, nan converted normally)
+// float -> double by bit splicing: exact for normal numbers; zero and
+// denormals give signed zero, inf/nan stay inf/nan (no FP64-pipe instruction)
 __device__ __forceinline__ double f2d_bits(float f)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned e = (u >> 23) & 0xFFu;
-    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (e == 0u || e == 0xFFu) return (double)f;
-    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)),
-                            (int)(u << 29));
+    const unsigned sign = u & 0x80000000u;
+    if (e == 0u) return __hiloint2double((int)sign, 0);
+    if (e == 0xFFu) return __hiloint2double((int)(sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3)), 0);
+    return __hiloint2double((int)(sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
 }
 
 // double -> (hi, lo) floats holding the top 48 significand bits, integer ops
-// only; values outside the float range take the ordinary conversion.
+// only; magnitudes outside the float range become 0 or inf.
 __device__ __forceinline__ void df_split(double x, float &hi, float &lo)
 {
     const int h = __double2hiint(x);
     const unsigned l = (unsigned)__double2loint(x);
     const unsigned sign = (unsigned)h & 0x80000000u;
     const int e = ((h >> 20) & 0x7FF) - 1023;
-    if (((h & 0x7FFFFFFF) | (int)l) == 0) { hi = 0.f; lo = 0.f; return; }
-    if (e < -125 || e > 127) { hi = (float)x; lo = 0.f; return; }
+    if (((h & 0x7FFFFFFF) | (int)l) == 0 || e < -125) {   // zero / below the float range
+        hi = __uint_as_float(sign); lo = 0.f; return;
+    }
+    if (e > 127) { hi = __uint_as_float(sign | 0x7F800000u); lo = 0.f; return; }   // inf
     hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (((unsigned)h & 0xFFFFFu) << 3) |
                          (l >> 29));
     const unsigned rem = l & 0x1FFFFFFFu;
@@ -168,15 +171,32 @@ __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
     const float beta = (float)a.beta;
     dfloat sm = {0.f, 0.f};
     float sv = 0.f, kv = 0.f, sd = 0.f, kd = 0.f;   // Kahan sums of var/n and d_h
+    const cvg_u64 *__restrict__ nhs = a.nh_sum;
+    double *__restrict__ JF = a.JF;
+    double *__restrict__ JF2 = a.JF2;
+    double *__restrict__ DH = a.dh;
+    // issue every load of this thread's cubes before any store
+    cvg_u64 s0[RIPT], s1[RIPT];
+    double j1[RIPT], j2[RIPT];
+#pragma unroll
+    for (int k = 0; k < RIPT; ++k) {
+        const cvg_u32 c = base + k * RB + threadIdx.x;
+        const bool in = c < a.n_cubes;
+        s0[k] = in ? nhs[c] : 0ull;
+        s1[k] = in ? nhs[c + 1] : 1ull;
+        j1[k] = in ? JF[c] : 0.0;
+        j2[k] = in ? JF2[c] : 0.0;
+    }
+#pragma unroll
     for (int k = 0; k < RIPT; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
-        const int neval = (int)(a.nh_sum[c + 1] - a.nh_sum[c]);
+        JF[c] = 0.0;
+        JF2[c] = 0.0;
+        const int neval = (int)(s1[k] - s0[k]);
         float jh, jl, qh, ql;
-        df_split(a.JF[c], jh, jl);
-        df_split(a.JF2[c], qh, ql);
-        a.JF[c] = 0.0;
-        a.JF2[c] = 0.0;
+        df_split(j1[k], jh, jl);
+        df_split(j2[k], qh, ql);
         const float fn = (float)neval;
         const float inv = 1.0f / fn;
         // m = JF/n, q = JF2/n as double-floats
@@ -200,7 +220,7 @@ __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
             const float y = dh - kd, t = sd + y;
             kd = (t - sd) - y; sd = t;
         }
-        a.dh[c] = f2d_bits(dh);
+        DH[c] = f2d_bits(dh);
     }
     // warp reduction in FP32 (double-float for the estimate)
     float v = sv - kv, d = sd - kd;
@@ -278,19 +298,26 @@ __global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
     if (mode == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
     if (mode == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;   // round the total down
     cvg_u64 tot = 0;
+    double dhv[RIPT];
+#pragma unroll
+    for (int k = 0; k < RIPT; ++k) {   // issue the loads first
+        const cvg_u32 c = base + k * RB + threadIdx.x;
+        dhv[k] = (mode != 1 && c < a.n_cubes) ? a.dh[c] : 0.0;
+    }
+#pragma unroll
     for (int k = 0; k < RIPT; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
         cvg_u32 nh;
         if (mode == 0) {
-            const double f = a.dh[c] / dsum;
+            const double f = dhv[k] / dsum;
             const double x = f * n_it;
             // (int) conversion of the reference: NaN -> 0, saturating above
             int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
             nh = ns < 2 ? 2u : (cvg_u32)ns;
             a.nh_new[c] = nh;
         } else if (mode == 2) {
-            const float x = d2f_bits(a.dh[c]) * scale;
+            const float x = d2f_bits(dhv[k]) * scale;
             const int ns = (x >= 0.f && x < 2147483520.f) ? (int)x : (x >= 2147483520.f ? 2147483520 : 0);
             nh = ns < 2 ? 2u : (cvg_u32)ns;
             a.nh_new[c] = nh;
