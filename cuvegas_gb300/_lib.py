@@ -26,8 +26,9 @@ EXPORTS = (
     "cvg_compile_integrand", "cvg_integrand_release", "cvg_integrate", "cvg_run_create",
     "cvg_run_destroy", "cvg_run_iterate", "cvg_run_step", "cvg_run_result", "cvg_run_sync",
     "cvg_run_get", "cvg_run_set", "cvg_run_info_get", "cvg_run_grad", "cvg_compile_check",
-    "cvg_run_last_fill_ms", "cvg_run_fill_times", "cvg_measure_peak",
+    "cvg_run_last_fill_ms", "cvg_run_fill_times", "cvg_measure_peak", "cvg_realloc_noalloc",
 )
+NOALLOC_MAX_CUBES = 262144
 
 
 class CuvegasError(RuntimeError):
@@ -102,6 +103,8 @@ def load():
             "cvg_run_last_fill_ms": [vp, C.POINTER(C.c_float)],
             "cvg_run_fill_times": [vp, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)],
             "cvg_measure_peak": [vp, C.c_int32, C.POINTER(C.c_double)],
+            "cvg_realloc_noalloc": [vp, vp, vp, C.c_uint32, C.c_double, C.c_double, C.c_int64,
+                                    C.c_int32, vp, vp, C.c_uint64, C.c_int32, vp],
         }
         for name, args in sig.items():
             fn = getattr(L, name)

@@ -73,6 +73,8 @@ uint64_t fnv1a(const std::string &s, uint64_t h = 1469598103934665603ull)
 
 }  // namespace
 
+void cvg_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
+
 struct cvg_context_s {
     int device = 0;
     cudaStream_t stream = nullptr;

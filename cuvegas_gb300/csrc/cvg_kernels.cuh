@@ -79,4 +79,7 @@ cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cuda
 // Fill n words with a value.
 cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
 
+// Set the calling thread's cvg_last_error() message (host code of the library).
+void cvg_internal_set_error(const char *msg);
+
 #endif

@@ -183,6 +183,31 @@ cvg_status cvg_run_last_fill_ms(cvg_run r, float *ms);
  * (CVG_FLAG_TIME_FILL); synchronises.  At most `cap` values; *n = count. */
 cvg_status cvg_run_fill_times(cvg_run r, float *ms, int32_t cap, int32_t *n);
 
+/* ---- reallocation without allocation ----
+ * For callers that cannot call cudaMalloc (code running inside another
+ * framework's memory pool, or with all device memory reserved up front).
+ * No counterpart in the reference: it allocates inside every call.
+ *
+ * Runs the same reallocation kernels as the iteration loop on caller-owned
+ * device buffers: JF/JF2 [n_cubes] (the fill's per-hypercube sums; read, then
+ * cleared to zero), nh_sum [n_cubes+1] (in: the exclusive prefix of the
+ * current per-cube sample counts; out: the reallocated prefix), est [3]
+ * (out: I, sigma^2 and samples of the iteration), and optionally tile_cube
+ * [max_tiles] (out: the cube of each tile's first sample, tiles of
+ * tile_samples; NULL skips it).  All temporaries live in one statically
+ * allocated __device__ array (about 3 MiB per GPU that loads the library,
+ * held until exit): n_cubes may not exceed CVG_NOALLOC_MAX_CUBES; larger
+ * calls are rejected.  Calls share that array, so calls that overlap on the
+ * GPU race.  The first call on a device looks up the array's address;
+ * make that first call before any stream capture.  Calls no cudaMalloc or
+ * cudaFree.  precision: CVG_PREC_FP64 (reference arithmetic) or
+ * CVG_PREC_FP32 (compensated FP32 per cube).  stream may be NULL. */
+#define CVG_NOALLOC_MAX_CUBES 262144
+cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_sum, uint32_t n_cubes,
+                               double v_cubes, double beta, int64_t n_eval_it, int32_t precision,
+                               double *est, uint32_t *tile_cube, uint64_t max_tiles,
+                               int32_t tile_samples, void *stream);
+
 /* Throughput microbenchmark of this device: kind 0 = FP32 FMA, 1 = FP64 FMA
  * (TFLOP/s, 2 flops per FMA), 2 = device-memory copy (GB/s, read+write). */
 cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out);
