@@ -35,6 +35,7 @@ struct cvg_fill_args {
     cvg_u32 *counts;              // [dim][N] samples per bin
     double *grad;                 // [n_params] dI/dtheta accumulator (gradient pass)
     cvg_u32 *status;              // error bits
+    int *scale_exp;               // FP32 form: f*jac is scaled by 2^-scale_exp (may be null)
     cvg_u64 max_tiles;            // capacity of tile_cube
     cvg_u64 seed;                 // Philox key
     cvg_u32 instance;             // Philox counter word 3, bits 8..31

@@ -72,6 +72,30 @@ CVG_D double cvg_f2d(float f)
 CVG_D double cvg_to_double(float f) { return cvg_f2d(f); }
 CVG_D double cvg_to_double(double f) { return f; }
 
+// f * 2^k widened to double by bit splicing (FP32 form: undoes the 2^-k
+// scaling of f*jac; k = 0 for FP64).  Overflow gives inf, underflow zero.
+CVG_D double cvg_to_double_scaled(float f, int k)
+{
+    const cvg_u32 u = __float_as_uint(f);
+    const int e = (int)((u >> 23) & 0xFFu);
+    const cvg_u32 sign = u & 0x80000000u;
+    if (e == 0) return __hiloint2double((int)sign, 0);
+    if (e == 0xFF) return __hiloint2double((int)(sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3)), 0);
+    const int E = e + 896 + k;
+    if (E <= 0) return __hiloint2double((int)sign, 0);
+    if (E >= 2047) return __hiloint2double((int)(sign | 0x7FF00000u), 0);
+    return __hiloint2double((int)(sign | ((cvg_u32)E << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
+}
+CVG_D double cvg_to_double_scaled(double f, int) { return f; }
+
+// 2^-k as T (FP32 form scale of f*jac; 1 for FP64)
+CVG_D float cvg_scale_pow2(float, int k)
+{
+    k = k < -126 ? -126 : (k > 126 ? 126 : k);
+    return __int_as_float((127 - k) << 23);
+}
+CVG_D double cvg_scale_pow2(double, int) { return 1.0; }
+
 // Bin of z = y*N (0 <= z <= N) and the fraction inside it:
 // b = min(floor(z), N-1), frac = z - b (src/main.cu:49-52).  The FP32 form
 // floors by a round-down add of 2^23 (no float/int conversion instruction).
@@ -169,6 +193,10 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     const T fNm1 = (T)(N - 1);
     const T *G = ESM ? E : grid;
     const T vc = (T)a.v_cubes;
+    // FP32 form: f*jac is carried as f*jac*2^-k so its square stays in range;
+    // sums are widened back with the exponent shift (exact)
+    const int kx = (sizeof(T) == 4 && a.scale_exp) ? *a.scale_exp : 0;
+    const T jac0 = cvg_scale_pow2((T)0, kx);
 
     cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
 #pragma unroll
@@ -226,8 +254,8 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 #pragma unroll
                             for (int p = 0; p < PP; ++p) { gacc[p].add(ag[p] * sc); ag[p] = (T)0; }
                         } else {
-                            const double v1 = cvg_to_double(a1.value_t());
-                            const double v2 = cvg_to_double(a2.value_t());
+                            const double v1 = cvg_to_double_scaled(a1.value_t(), kx);
+                            const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * kx);
                             if (cstart >= l0) { a.JF[c] = v1; a.JF2[c] = v2; }
                             else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
                             a1.reset(); a2.reset();
@@ -254,7 +282,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
                 }
                 T x[D];
                 int bin[D];
-                T jac = (T)1;
+                T jac = jac0;
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
                     T u;
@@ -302,8 +330,8 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 #pragma unroll
                     for (int p = 0; p < PP; ++p) gacc[p].add(ag[p] * sc);
                 } else {
-                    const double v1 = cvg_to_double(a1.value_t());
-                    const double v2 = cvg_to_double(a2.value_t());
+                    const double v1 = cvg_to_double_scaled(a1.value_t(), kx);
+                    const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * kx);
                     if (cstart >= l0 && next == lend) { a.JF[c] = v1; a.JF2[c] = v2; }
                     else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
                 }
@@ -326,7 +354,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
         const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
         for (int p = 0; p < PP; ++p) {
-            double v = gacc[p].value();
+            double v = ldexp(gacc[p].value(), kx);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
             if (lane == 0) red[warp * PP + p] = v;
@@ -338,6 +366,55 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
             atomicAdd(&a.grad[tid], v);
         }
     }
+}
+
+// Pilot for the FP32 form's scale: the binary exponent of max |f*jac| over
+// one sample in each of the first cubes (grid as it is now, Philox counter
+// word 2 = 0xFFFFFFFF so no iteration's samples are reused).  Results are
+// combined with atomicMax into *a.scale_exp (initialised by the host).
+template <int D, typename T, int BS, int P>
+CVG_D void cvg_pilot_body(const cvg_fill_args &a)
+{
+    __shared__ T th[P > 0 ? P : 1];
+    for (int i = threadIdx.x; i < P; i += BS) th[i] = (T)a.theta[i];
+    __syncthreads();
+    const cvg_u32 gid = blockIdx.x * BS + threadIdx.x;
+    const cvg_u32 c = gid % a.n_cubes;
+    const cvg_u32 j = gid / a.n_cubes;
+    const int N = a.n_intervals, ns = a.n_strat;
+    const T dy = (T)1 / (T)ns, fN = (T)N, fNm1 = (T)(N - 1);
+    const T *grid = cvg_grid_src<T>::get(a);
+    int coord[D];
+    T cdy[D];
+    cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
+    constexpr int NB = (D + 3) / 4;
+    cvg_u32 rr[NB * 4];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const cvg_u32x4 r4 = cvg_philox(j, c, 0xFFFFFFFFu, (cvg_u32)b | (a.instance << 8),
+                                        (cvg_u32)a.seed, (cvg_u32)(a.seed >> 32));
+        rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y; rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
+    }
+    T x[D];
+    T jac = (T)1;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const T y = cvg_fma(cvg_uniform<T>(rr[d]), dy, cdy[d]);
+        const T z = y * fN;
+        T frac;
+        const int b = cvg_bin(z, N, fNm1, frac);
+        const T e0 = grid[d * (N + 1) + b], dx = grid[d * (N + 1) + b + 1] - e0;
+        x[d] = cvg_fma(dx, frac, e0);
+        jac *= fN * dx;
+    }
+    const T v = (T)CVG_F(x, th) * jac;
+    const float fv = fabsf((float)v);
+    int e = -200;
+    if (fv > 0.f && fv <= 3.4e38f) e = (int)((__float_as_uint(fv) >> 23) & 0xFFu) - 127;
+    else if (!(fv <= 3.4e38f)) e = 128;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(a.scale_exp, e);
 }
 
 #endif  // CVG_FILL_CUH

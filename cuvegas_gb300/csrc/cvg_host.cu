@@ -95,6 +95,7 @@ struct cvg_integrand_s {
 
 struct fill_variant {
     cudaKernel_t kernel = nullptr;
+    cudaKernel_t pilot = nullptr;
     size_t smem = 0;
     int occ = 0;
 };
@@ -119,6 +120,7 @@ struct cvg_run_s {
     float *x_edges32 = nullptr, *ubuf = nullptr;
     cvg_u32 *counts = nullptr, *nh_new = nullptr, *tile_cube = nullptr, *iteration = nullptr;
     cvg_u32 *status = nullptr;
+    int *scale_exp = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
     size_t ubuf_samples = 0;
@@ -205,13 +207,15 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
         s += "#define CVG_HAS_GRAD 1\n#define CVG_DF(x, th, g) integrand_grad(x, th, g)\n";
     }
     s += cvg_src_fill;
-    char entry[512];
+    char entry[1024];
     std::snprintf(entry, sizeof(entry),
                   "\nextern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_entry("
-                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s>(a); }\n",
+                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s>(a); }\n"
+                  "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_entry("
+                  "const cvg_fill_args a) { cvg_pilot_body<%d, %s, 256, %d>(a); }\n",
                   k.block, k.dim, T, k.block, k.esm ? "true" : "false",
                   k.hsm ? "true" : "false", k.replay ? "true" : "false", k.n_params,
-                  k.grad ? "true" : "false");
+                  k.grad ? "true" : "false", k.dim, T, k.n_params);
     s += entry;
     return s;
 }
@@ -252,7 +256,7 @@ std::vector<std::string> nvrtc_options(const std::string &arch)
 }
 
 cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_key &k,
-                      cudaKernel_t *out)
+                      cudaKernel_t *out, cudaKernel_t *pilot = nullptr)
 {
     const std::string src = make_source(f, k);
     const std::vector<std::string> opts = nvrtc_options(ctx->arch);
@@ -286,6 +290,7 @@ cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_k
         ctx->libs[key] = lib;
     }
     CK(cudaLibraryGetKernel(out, lib, "cvg_fill_entry"));
+    if (pilot) CK(cudaLibraryGetKernel(pilot, lib, "cvg_pilot_entry"));
     return CVG_OK;
 }
 
@@ -298,7 +303,7 @@ cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v
     if (grad) k.hsm = 0;
     const cvg_u64 smem = cvg_fill_smem_bytes(k.dim, r->p.n_intervals, tsz, k.esm, k.hsm, k.grad,
                                              r->TS, k.n_params, k.block);
-    CKS(jit_kernel(ctx, *r->f, k, &v->kernel));
+    CKS(jit_kernel(ctx, *r->f, k, &v->kernel, &v->pilot));
     const void *fn = (const void *)v->kernel;
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
@@ -342,6 +347,7 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.acc = r->acc;
     a.iteration = r->iteration;
     a.status = r->status;
+    a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
     a.max_tiles = r->max_tiles;
     a.n_eval_it = r->n_eval_it;
     a.v_cubes = r->v_cubes;
@@ -385,6 +391,7 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.counts = r->counts;
     a.grad = r->grad;
     a.status = r->status;
+    a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
     a.max_tiles = r->max_tiles;
     a.seed = r->p.seed;
     a.instance = r->p.instance;
@@ -425,6 +432,25 @@ cvg_status launch_fill(cvg_run_s *r, const fill_variant &v, bool timed)
         r->ev0 = e0;
         r->ev1 = e1;
     }
+    return CVG_OK;
+}
+
+// FP32 form: choose the scale exponent of f*jac from a pilot evaluation
+cvg_status run_pilot(cvg_run_s *r)
+{
+    const int init = -1000;
+    cudaStream_t st = r->ctx->stream;
+    CK(cudaMemcpyAsync(r->scale_exp, &init, sizeof(int), cudaMemcpyHostToDevice, st));
+    cvg_fill_args a = fill_args(r);
+    void *args[] = {&a};
+    const cvg_u64 pts = std::min<cvg_u64>((cvg_u64)r->ctx->n_sm * 1024, 4ull * r->n_cubes + 255);
+    const unsigned blocks = (unsigned)((pts + 255) / 256);
+    CK(cudaLaunchKernel((const void *)r->fill.pilot, dim3(blocks), dim3(256), args, 0, st));
+    int e = 0;
+    CK(cudaMemcpyAsync(&e, r->scale_exp, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    e = e < -100 ? 0 : (e > 100 ? 100 : e);   // no finite nonzero value seen: no scaling
+    CK(cudaMemcpyAsync(r->scale_exp, &e, sizeof(int), cudaMemcpyHostToDevice, st));
     return CVG_OK;
 }
 
@@ -606,12 +632,13 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->nh_sum, sizeof(cvg_u64) * ((size_t)r->n_cubes + 1)},
         {(void **)&r->nh_new, sizeof(cvg_u32) * r->n_cubes},
         {(void **)&r->tile_cube, sizeof(cvg_u32) * r->max_tiles},
-        {(void **)&r->partials, sizeof(double) * 3 * r->nb},
+        {(void **)&r->partials, sizeof(double) * 4 * r->nb},
         {(void **)&r->bsums, sizeof(cvg_u64) * (r->nb + 1)},
         {(void **)&r->stats, sizeof(double) * 3 * p.max_it},
         {(void **)&r->acc, sizeof(cvg_acc_dev)},
         {(void **)&r->iteration, sizeof(cvg_u32)},
         {(void **)&r->status, sizeof(cvg_u32)},
+        {(void **)&r->scale_exp, sizeof(int)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
     };
@@ -657,6 +684,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cvg_launch_fill_u32(r->nh_new, (cvg_u32)nh0, r->n_cubes, st));
     CK(cvg_launch_set_nh(realloc_args(r), r->nh_new, st));
     CKS(prepare_variant(r, false, false, &r->fill));
+    CK(cudaMemsetAsync(r->scale_exp, 0, sizeof(int), st));
+    if (p.precision == CVG_PREC_FP32) CKS(run_pilot(r));
     CK(cudaStreamSynchronize(st));
     return CVG_OK;
 }
@@ -814,6 +843,7 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     case CVG_BUF_THETA: src = r->theta; need = sizeof(double) * r->f->n_params; break;
     case CVG_BUF_ITERATION: src = r->iteration; need = sizeof(cvg_u32); break;
     case CVG_BUF_STATS: src = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
+    case CVG_BUF_SCALE_EXP: src = r->scale_exp; need = sizeof(int); break;
     default: return fail(CVG_ERR_INVALID, "unknown buffer");
     }
     if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
@@ -853,6 +883,7 @@ cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes)
     case CVG_BUF_COUNTS: dst = r->counts; need = sizeof(cvg_u32) * D * N; break;
     case CVG_BUF_THETA: dst = r->theta; need = sizeof(double) * r->f->n_params; break;
     case CVG_BUF_ITERATION: dst = r->iteration; need = sizeof(cvg_u32); break;
+    case CVG_BUF_SCALE_EXP: dst = r->scale_exp; need = sizeof(int); break;
     case CVG_BUF_UNIFORMS: {
         if (bytes == 0) { r->replay = false; return CVG_OK; }
         if (!host || bytes % (sizeof(float) * D)) return fail(CVG_ERR_INVALID, "uniforms: [S][dim] floats");

@@ -85,15 +85,15 @@ __device__ __forceinline__ double f2d_bits(float f)
     return __hiloint2double((int)(sign | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3)), (int)(u << 29));
 }
 
-// double -> (hi, lo) floats holding the top 48 significand bits, integer ops
-// only; magnitudes outside the float range become 0 or inf.
-__device__ __forceinline__ void df_split(double x, float &hi, float &lo)
+// x * 2^shift -> (hi, lo) floats holding the top 48 significand bits, integer
+// ops only; magnitudes outside the float range become 0 or inf.
+__device__ __forceinline__ void df_split(double x, float &hi, float &lo, int shift = 0)
 {
     const int h = __double2hiint(x);
     const unsigned l = (unsigned)__double2loint(x);
     const unsigned sign = (unsigned)h & 0x80000000u;
-    const int e = ((h >> 20) & 0x7FF) - 1023;
-    if (((h & 0x7FFFFFFF) | (int)l) == 0 || e < -125) {   // zero / below the float range
+    const int e = ((h >> 20) & 0x7FF) - 1023 + shift;   // x * 2^shift
+    if (((h & 0x7FFFFFFF) | (int)l) == 0 || e < -125 || ((h >> 20) & 0x7FF) == 0) {   // zero, tiny
         hi = __uint_as_float(sign); lo = 0.f; return;
     }
     if (e > 127) { hi = __uint_as_float(sign | 0x7F800000u); lo = 0.f; return; }   // inf
@@ -153,9 +153,10 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
     }
     block_sum<3>(v, scratch);
     if (threadIdx.x == 0) {
-        a.partials[3 * blockIdx.x + 0] = v[0];
-        a.partials[3 * blockIdx.x + 1] = v[1];
-        a.partials[3 * blockIdx.x + 2] = v[2];
+        a.partials[4 * blockIdx.x + 0] = v[0];
+        a.partials[4 * blockIdx.x + 1] = v[1];
+        a.partials[4 * blockIdx.x + 2] = v[2];
+        a.partials[4 * blockIdx.x + 3] = 0.0;
     }
 }
 
@@ -166,11 +167,13 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
 // k3_finish multiplies by V and V^2.
 __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
 {
-    __shared__ double wsum[3][RB / 32];
+    __shared__ double wsum[4][RB / 32];
     const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
     const float beta = (float)a.beta;
+    const int kx = a.scale_exp ? *a.scale_exp : 0;   // work on JF*2^-k, JF2*2^-2k
     dfloat sm = {0.f, 0.f};
     float sv = 0.f, kv = 0.f, sd = 0.f, kd = 0.f;   // Kahan sums of var/n and d_h
+    float sq = 0.f;                                  // sum of JF2*2^-2k (next scale)
     const cvg_u64 *__restrict__ nhs = a.nh_sum;
     double *__restrict__ JF = a.JF;
     double *__restrict__ JF2 = a.JF2;
@@ -195,8 +198,9 @@ __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
         JF2[c] = 0.0;
         const int neval = (int)(s1[k] - s0[k]);
         float jh, jl, qh, ql;
-        df_split(j1[k], jh, jl);
-        df_split(j2[k], qh, ql);
+        df_split(j1[k], jh, jl, -kx);
+        df_split(j2[k], qh, ql, -2 * kx);
+        sq += qh;
         const float fn = (float)neval;
         const float inv = 1.0f / fn;
         // m = JF/n, q = JF2/n as double-floats
@@ -230,39 +234,56 @@ __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
         sm = df_add(sm, other);
         v += __shfl_down_sync(0xffffffffu, v, o);
         d += __shfl_down_sync(0xffffffffu, d, o);
+        sq += __shfl_down_sync(0xffffffffu, sq, o);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
         wsum[0][warp] = f2d_bits(d);
         wsum[1][warp] = f2d_bits(sm.h) + f2d_bits(sm.l);
         wsum[2][warp] = f2d_bits(v);
+        wsum[3][warp] = f2d_bits(sq);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t0 = 0.0, t1 = 0.0, t2 = 0.0;
-        for (int w = 0; w < RB / 32; ++w) { t0 += wsum[0][w]; t1 += wsum[1][w]; t2 += wsum[2][w]; }
-        a.partials[3 * blockIdx.x + 0] = t0;
-        a.partials[3 * blockIdx.x + 1] = t1;
-        a.partials[3 * blockIdx.x + 2] = t2;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        for (int w = 0; w < RB / 32; ++w) {
+            t0 += wsum[0][w]; t1 += wsum[1][w]; t2 += wsum[2][w]; t3 += wsum[3][w];
+        }
+        a.partials[4 * blockIdx.x + 0] = t0;
+        a.partials[4 * blockIdx.x + 1] = t1;
+        a.partials[4 * blockIdx.x + 2] = t2;
+        a.partials[4 * blockIdx.x + 3] = t3;
     }
 }
 
 __global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned nb)
 {
-    __shared__ double scratch[3 * 32];
-    double v[3] = {0.0, 0.0, 0.0};
+    __shared__ double scratch[4 * 32];
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
     for (unsigned i = threadIdx.x; i < nb; i += blockDim.x) {
-        v[0] += a.partials[3 * i + 0];
-        v[1] += a.partials[3 * i + 1];
-        v[2] += a.partials[3 * i + 2];
+        v[0] += a.partials[4 * i + 0];
+        v[1] += a.partials[4 * i + 1];
+        v[2] += a.partials[4 * i + 2];
+        v[3] += a.partials[4 * i + 3];
     }
-    block_sum<3>(v, scratch);
+    block_sum<4>(v, scratch);
     if (threadIdx.x == 0) {
         const cvg_u32 it = *a.iteration;
         double r = v[1], s = v[2];
-        if (a.fast_pow) {   // FP32 form sums m and var/n without the cube volume
-            r *= a.v_cubes;
-            s *= a.v_cubes * a.v_cubes;
+        if (a.fast_pow) {   // FP32 form sums m 2^-k and var 2^-2k / n without the cube volume
+            const int kx = a.scale_exp ? *a.scale_exp : 0;
+            r = ldexp(r, kx) * a.v_cubes;
+            s = ldexp(s, 2 * kx) * (a.v_cubes * a.v_cubes);
+            if (a.scale_exp) {   // next scale: 2^k ~ rms of f*jac
+                const double ms = v[3] / (double)a.nh_sum[a.n_cubes];
+                if (ms > 0.0 && isfinite(ms)) {
+                    int e = 0;
+                    frexp(ms, &e);
+                    int knew = kx + e / 2;
+                    knew = knew < -100 ? -100 : (knew > 100 ? 100 : knew);
+                    *a.scale_exp = knew;
+                }
+            }
         }
         if ((int)it < a.max_it) {
             a.stats[it] = r;

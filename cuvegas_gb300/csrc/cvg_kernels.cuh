@@ -27,13 +27,14 @@ struct cvg_realloc_args {
     double *JF, *JF2;       // [n_cubes], read then zeroed
     double *dh;             // [n_cubes]
     cvg_u32 *nh_new;        // [n_cubes]
-    double *partials;       // [n_blocks][3]
+    double *partials;       // [n_blocks][4]
     cvg_u64 *bsums;         // [n_blocks]
     cvg_u32 *tile_cube;     // [max_tiles]
     double *stats;          // [2*max_it]
     cvg_acc_dev *acc;
     cvg_u32 *iteration;
     cvg_u32 *status;
+    int *scale_exp;         // FP32 form: scale exponent k of the fill (updated here); may be null
     cvg_u64 max_tiles;
     cvg_i64 n_eval_it;
     double v_cubes;

@@ -35,7 +35,7 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffDh = 0;
 constexpr size_t kOffNh = kOffDh + align256(sizeof(double) * kMaxCubes);
 constexpr size_t kOffPart = kOffNh + align256(sizeof(cvg_u32) * kMaxCubes);
-constexpr size_t kOffBsum = kOffPart + align256(sizeof(double) * 3 * kMaxBlocks);
+constexpr size_t kOffBsum = kOffPart + align256(sizeof(double) * 4 * kMaxBlocks);
 constexpr size_t kOffAcc = kOffBsum + align256(sizeof(cvg_u64) * (kMaxBlocks + 1));
 constexpr size_t kOffIt = kOffAcc + align256(sizeof(cvg_acc_dev));
 constexpr size_t kOffStatus = kOffIt + 256;
@@ -98,6 +98,7 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
     a.acc = (cvg_acc_dev *)(b + kOffAcc);
     a.iteration = (cvg_u32 *)(b + kOffIt);
     a.status = (cvg_u32 *)(b + kOffStatus);
+    a.scale_exp = nullptr;               // JF/JF2 are taken at their own magnitude
     a.stats = est;                       // est[0] = I, est[1] = sigma^2, est[2] = samples
     a.tile_cube = tile_cube;
     a.max_tiles = tile_cube ? max_tiles : 0;

@@ -151,7 +151,10 @@ enum {
     CVG_BUF_UNIFORMS = 10,   /* float  [S][dim]          set: replay these uniforms in
                                 the next fills instead of Philox (parity tests); 0 bytes
                                 switches back                                         */
-    CVG_BUF_STATS = 11       /* double [3][max_it]       get: I_it, sigma2_it, samples_it */
+    CVG_BUF_STATS = 11,      /* double [3][max_it]       get: I_it, sigma2_it, samples_it */
+    CVG_BUF_SCALE_EXP = 12   /* int32  [1]               get/set: FP32 form carries f*jac
+                                scaled by 2^-k (k chosen by a pilot, then updated each
+                                iteration) so (f*jac)^2 stays in float range             */
 };
 cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
 cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);

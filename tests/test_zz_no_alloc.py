@@ -42,6 +42,8 @@ def test_noalloc_matches_run_step_twice(ctx, prec):
         info = r.info
         assert info.n_cubes <= L.NOALLOC_MAX_CUBES
         nh_sum0 = r.get(L.BUF_NH_SUM)
+        # the entry point takes JF/JF2 at their own magnitude (scale exponent 0)
+        r.set(L.BUF_SCALE_EXP, np.array([0], dtype=np.int32))
         r.set(L.BUF_JF, o.JF)
         r.set(L.BUF_JF2, o.JF2)
         r.step(L.STAGE_REALLOC)
