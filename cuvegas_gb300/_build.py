@@ -18,7 +18,7 @@ LIB = os.path.join(LIBDIR, "libcuvegas.so")
 INCLUDE = os.path.join(ROOT, "include")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EMBED = ["cvg_common.cuh", "cvg_fill.cuh"]
-UNITS = ["cvg_kernels.cu", "cvg_host.cu", "cvg_noalloc.cu"]
+UNITS = ["cvg_kernels.cu", "cvg_host.cu", "cvg_noalloc.cu", "cvg_batch.cu"]
 
 
 def cuda_home():

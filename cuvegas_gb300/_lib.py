@@ -27,6 +27,8 @@ EXPORTS = (
     "cvg_run_destroy", "cvg_run_iterate", "cvg_run_step", "cvg_run_result", "cvg_run_sync",
     "cvg_run_get", "cvg_run_set", "cvg_run_info_get", "cvg_run_grad", "cvg_compile_check",
     "cvg_run_last_fill_ms", "cvg_run_fill_times", "cvg_measure_peak", "cvg_realloc_noalloc",
+    "cvg_batch_create", "cvg_batch_destroy", "cvg_batch_iterate", "cvg_batch_results",
+    "cvg_batch_info_get", "cvg_batch_last_fill_ms", "cvg_batch_compile_check",
 )
 NOALLOC_MAX_CUBES = 262144
 
@@ -53,6 +55,11 @@ class Result(C.Structure):
                 ("seed", C.c_uint64), ("gpu_thr", C.c_double), ("chi2_dof", C.c_double),
                 ("n_it_used", C.c_int32), ("n_it_done", C.c_int32), ("precision", C.c_int32),
                 ("pad", C.c_int32)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("n_dim", C.c_int32), ("n_strat", C.c_int32), ("tot_eval", C.c_int64),
+                ("instance", C.c_uint32), ("pad", C.c_int32)]
 
 
 class RunInfo(C.Structure):
@@ -105,6 +112,17 @@ def load():
             "cvg_measure_peak": [vp, C.c_int32, C.POINTER(C.c_double)],
             "cvg_realloc_noalloc": [vp, vp, vp, C.c_uint32, C.c_double, C.c_double, C.c_int64,
                                     C.c_int32, vp, vp, C.c_uint64, C.c_int32, vp],
+            "cvg_batch_create": [vp, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(Instance),
+                                 C.POINTER(C.c_int32), vp, C.POINTER(Params), C.POINTER(vp)],
+            "cvg_batch_destroy": [vp],
+            "cvg_batch_iterate": [vp, C.c_int32],
+            "cvg_batch_results": [vp, C.POINTER(Result), vp, vp],
+            "cvg_batch_info_get": [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+            "cvg_batch_last_fill_ms": [vp, C.POINTER(C.c_float)],
+            "cvg_batch_compile_check": [C.c_char_p, C.c_int32, C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.c_char_p,
+                                        C.c_char_p, sz],
         }
         for name, args in sig.items():
             fn = getattr(L, name)
@@ -135,6 +153,20 @@ def compile_check(source, n_dim, precision=PREC_FP64, n_params=0, has_grad=False
     log = C.create_string_buffer(1 << 16)
     s = L.cvg_compile_check(source.encode(), n_dim, abi, n_params, int(bool(has_grad)),
                             precision, arch.encode(), log, len(log))
+    if s != OK:
+        raise CuvegasError(s, last_error())
+    return log.value.decode(errors="replace")
+
+
+def batch_compile_check(source, dims, params_per_dim, precision=PREC_FP32, block=512,
+                        arch="sm_103a"):
+    """NVRTC-only compile of the batched kernels (no GPU needed)."""
+    L = load()
+    log = C.create_string_buffer(1 << 16)
+    d = (C.c_int32 * len(dims))(*dims)
+    ppd = (C.c_int32 * 17)(*params_per_dim)
+    s = L.cvg_batch_compile_check(source.encode(), len(dims), d, ppd, precision, block,
+                                  arch.encode(), log, len(log))
     if s != OK:
         raise CuvegasError(s, last_error())
     return log.value.decode(errors="replace")

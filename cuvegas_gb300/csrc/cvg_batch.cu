@@ -1,0 +1,551 @@
+// cvg_batch.cu -- many independent VEGAS+ integrals advanced together.
+//
+// Instances share one integrand family (one source, parameters theta per
+// instance) but differ in dimension, evaluation count and parameters.  Per
+// iteration the GPU runs, for the whole batch:
+//   one persistent fill launch (tiles of every instance, dimensions
+//   dispatched inside the kernel), the batched grid refinement (a cluster per
+//   instance and dimension) and the batched reallocation (blocks of every
+//   instance), which also numbers the tiles of the next fill.
+// With CVG_FLAG_GRAPH the iteration is captured once as a CUDA graph and
+// replayed.  Each instance reproduces a single-instance run with the same
+// seed and instance id (same Philox samples, same arithmetic).
+#include "cuvegas.h"
+#include "cvg_internal.h"
+#include "cvg_kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <set>
+#include <string>
+#include <vector>
+
+#define BCK(x)                                                                       \
+    do {                                                                             \
+        cudaError_t e_ = (x);                                                        \
+        if (e_ != cudaSuccess)                                                       \
+            return cvg_internal_fail(e_ == cudaErrorMemoryAllocation ? CVG_ERR_NOMEM \
+                                                                     : CVG_ERR_CUDA, \
+                                     std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+#define BCKS(x)                      \
+    do {                             \
+        cvg_status s_ = (x);         \
+        if (s_ != CVG_OK) return s_; \
+    } while (0)
+
+namespace {
+
+struct inst_host {
+    int dim = 0, n_strat = 0, n_params = 0;
+    int64_t n_eval_it = 0;
+    cvg_u32 n_cubes = 0;
+    double v_cubes = 0.0;
+    unsigned nb = 0;
+    cvg_u64 max_tiles = 0;
+    cvg_u32 nh0 = 0;
+    // device pointers
+    double *x_edges, *weights, *JF, *JF2, *dh, *partials, *stats, *theta, *grad;
+    float *x_edges32;
+    cvg_u32 *counts, *nh_new, *tile_cube, *iteration;
+    int *scale_exp;
+    cvg_u64 *nh_sum, *bsums;
+    cvg_acc_dev *acc;
+};
+
+}  // namespace
+
+struct cvg_batch_s {
+    cvg_context ctx = nullptr;
+    cvg_integrand_s f;
+    cvg_params p{};
+    int n = 0, block = 0, spt = 0, TS = 0, grid = 0, it_done = 0;
+    std::vector<inst_host> inst;
+    std::vector<int> params_per_dim;
+    void *arena = nullptr;
+    // device tables
+    cvg_fill_args *d_fill = nullptr;
+    cvg_realloc_args *d_realloc = nullptr;
+    cvg_refine_args *d_refine = nullptr;
+    int *d_dims = nullptr;
+    unsigned *d_blk_base = nullptr, *d_dim_base = nullptr;
+    cvg_u64 *d_tile_base = nullptr;
+    cvg_u32 *d_status = nullptr;
+    unsigned total_blocks = 0, total_dims = 0;
+    cudaKernel_t fill = nullptr, pilot = nullptr;
+    size_t fill_smem = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
+{
+    const char *T = b.p.precision == CVG_PREC_FP32 ? "float" : "double";
+    std::string s = "#define CVG_JIT 1\n";
+    s += cvg_internal_src_common();
+    for (int d : dims) {
+        s += "\nnamespace cvg_d" + std::to_string(d) + " {\nstatic constexpr int cvg_n_dim = " +
+             std::to_string(d) + ";\n#line 1 \"integrand.cu\"\n" + b.f.source + "\n}\n";
+    }
+    s += "#line 1 \"cvg_batch_adaptor\"\n";
+    s += cvg_internal_src_fill();
+    for (int d : dims)
+        s += cvg_internal_fn_struct(("cvg_fn_d" + std::to_string(d)).c_str(), b.f, b.f.abi,
+                                    b.params_per_dim[d], 0, "cvg_d" + std::to_string(d) + "::");
+    s += "struct cvg_disp {\n  template <int D> struct sel;\n"
+         "  template <int D> using fn = typename sel<D>::type;\n"
+         "  template <class Op> static __device__ __forceinline__ void run(int dim, Op &&op) {\n"
+         "    switch (dim) {\n";
+    for (int d : dims)
+        s += "      case " + std::to_string(d) + ": op(cvg_int<" + std::to_string(d) +
+             ">{}, cvg_int<" + std::to_string(b.params_per_dim[d]) + ">{}); break;\n";
+    s += "      default: break;\n    }\n  }\n};\n";
+    for (int d : dims)
+        s += "template <> struct cvg_disp::sel<" + std::to_string(d) + "> { using type = cvg_fn_d" +
+             std::to_string(d) + "; };\n";
+    char entry[512];
+    std::snprintf(entry, sizeof(entry),
+                  "extern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_batch_entry("
+                  "const cvg_batch_args b) { cvg_fill_batch<%s, %d, cvg_disp>(b); }\n"
+                  "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_batch_entry("
+                  "const cvg_batch_args b) { cvg_pilot_batch<%s, 8, cvg_disp>(b); }\n",
+                  b.block, T, b.block, T);
+    s += entry;
+    return s;
+}
+
+cvg_batch_args batch_args(const cvg_batch_s *b)
+{
+    cvg_batch_args a{};
+    a.inst = b->d_fill;
+    a.dims = b->d_dims;
+    a.tile_base = b->d_tile_base;
+    a.n_inst = b->n;
+    return a;
+}
+
+cvg_realloc_batch realloc_batch(const cvg_batch_s *b)
+{
+    cvg_realloc_batch B{};
+    B.A = b->d_realloc;
+    B.blk_base = b->d_blk_base;
+    B.total_blocks = b->total_blocks;
+    B.n = b->n;
+    return B;
+}
+
+cvg_refine_batch refine_batch(const cvg_batch_s *b)
+{
+    cvg_refine_batch B{};
+    B.R = b->d_refine;
+    B.dim_base = b->d_dim_base;
+    B.total_dims = b->total_dims;
+    B.n = b->n;
+    return B;
+}
+
+cvg_status enqueue_iteration(cvg_batch_s *b, bool timed)
+{
+    cudaStream_t s = b->ctx->stream;
+    cvg_batch_args ba = batch_args(b);
+    void *args[] = {&ba};
+    if (timed) BCK(cudaEventRecord(b->ev0, s));
+    BCK(cudaLaunchKernel((const void *)b->fill, dim3(b->grid), dim3(b->block), args, b->fill_smem, s));
+    if (timed) BCK(cudaEventRecord(b->ev1, s));
+    BCK(cvg_launch_refine_batch(refine_batch(b), b->p.n_intervals, s));
+    BCK(cvg_launch_realloc_batch(realloc_batch(b), (b->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1,
+                                 b->p.precision == CVG_PREC_FP32, b->d_tile_base, s));
+    return CVG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, int32_t n,
+                            const cvg_instance *insts, const int32_t *params_per_dim,
+                            const double *theta, const cvg_params *common, cvg_batch *out)
+{
+    if (!ctx || !source || !insts || !params_per_dim || !common || !out)
+        return cvg_internal_fail(CVG_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    if (n < 1 || n > 65536) return cvg_internal_fail(CVG_ERR_INVALID, "batch size must be in [1, 65536]");
+    const cvg_params &p = *common;
+    if (p.max_it < 1 || p.skip < 0 || p.n_intervals < 2 || p.n_intervals > CVG_REFINE_MAX_N)
+        return cvg_internal_fail(CVG_ERR_INVALID, "bad max_it / skip / n_intervals");
+    if (p.precision != CVG_PREC_FP64 && p.precision != CVG_PREC_FP32)
+        return cvg_internal_fail(CVG_ERR_INVALID, "bad precision");
+    if (abi != CVG_ABI_NATIVE) return cvg_internal_fail(CVG_ERR_INVALID, "batches take the native integrand ABI");
+    auto *b = new cvg_batch_s();
+    b->ctx = ctx;
+    b->f.ctx = ctx;
+    b->f.source = source;
+    b->f.abi = abi;
+    b->p = p;
+    b->n = n;
+    b->params_per_dim.assign(params_per_dim, params_per_dim + 17);
+    b->block = p.block > 0 ? p.block : 512;
+    b->spt = p.spt > 0 ? p.spt : 8;
+    if (b->block % 32 || b->block > 1024 || b->spt < 1 || b->spt > 256) {
+        delete b;
+        return cvg_internal_fail(CVG_ERR_INVALID, "bad block / spt");
+    }
+    b->TS = b->block * b->spt;
+    const int N = p.n_intervals;
+    std::set<int> dims;
+    int dmax = 0, pmax = 0;
+    b->inst.resize(n);
+    size_t total = 0;
+    auto seg = [](size_t bytes) { return (bytes + 255) & ~(size_t)255; };
+    for (int i = 0; i < n; ++i) {
+        inst_host &h = b->inst[i];
+        const cvg_instance &in = insts[i];
+        if (in.n_dim < 1 || in.n_dim > 16 || in.tot_eval < 1) {
+            delete b;
+            return cvg_internal_fail(CVG_ERR_INVALID, "instance " + std::to_string(i) +
+                                                          ": n_dim must be in [1, 16], tot_eval >= 1");
+        }
+        h.dim = in.n_dim;
+        h.n_params = params_per_dim[in.n_dim];
+        h.n_eval_it = in.tot_eval / p.max_it;
+        h.n_strat = in.n_strat > 0 ? in.n_strat : (int)std::pow((double)h.n_eval_it / 4.0, 1.0 / h.dim);
+        if (h.n_strat < 1) { delete b; return cvg_internal_fail(CVG_ERR_INVALID, "instance " + std::to_string(i) + ": too few evaluations"); }
+        const double nc = std::pow((double)h.n_strat, (double)h.dim);
+        const cvg_u64 s_max = (cvg_u64)h.n_eval_it + 2ull * (cvg_u64)nc;
+        if (nc > 4294967295.0 || s_max >= (1ull << 31) - (1ull << 20)) {
+            delete b;
+            return cvg_internal_fail(CVG_ERR_INVALID, "instance " + std::to_string(i) + " too large");
+        }
+        h.n_cubes = (cvg_u32)nc;
+        h.v_cubes = std::pow(1.0 / h.n_strat, (double)h.dim);
+        h.nh0 = (cvg_u32)std::max<int64_t>(2, (int64_t)(1.0 / (double)h.n_cubes * (double)h.n_eval_it));
+        h.nb = cvg_realloc_blocks(h.n_cubes);
+        h.max_tiles = (s_max + b->TS - 1) / b->TS + 1;
+        dims.insert(h.dim);
+        dmax = std::max(dmax, h.dim);
+        pmax = std::max(pmax, h.n_params);
+        const int D = h.dim;
+        total += seg(sizeof(double) * D * (N + 1)) + seg(sizeof(float) * D * (N + 1)) +
+                 seg(sizeof(double) * D * N) + seg(sizeof(cvg_u32) * D * N) +
+                 3 * seg(sizeof(double) * h.n_cubes) + seg(sizeof(cvg_u64) * (h.n_cubes + 1ull)) +
+                 seg(sizeof(cvg_u32) * h.n_cubes) + seg(sizeof(cvg_u32) * h.max_tiles) +
+                 seg(sizeof(double) * 4 * h.nb) + seg(sizeof(cvg_u64) * (h.nb + 1)) +
+                 seg(sizeof(double) * 3 * p.max_it) + seg(sizeof(cvg_acc_dev)) + 3 * seg(16) +
+                 2 * seg(sizeof(double) * std::max(1, h.n_params));
+    }
+    total += seg(sizeof(cvg_fill_args) * n) + seg(sizeof(cvg_realloc_args) * n) +
+             seg(sizeof(cvg_refine_args) * n) + seg(sizeof(int) * n) + 2 * seg(sizeof(unsigned) * (n + 1)) +
+             seg(sizeof(cvg_u64) * (n + 1)) + seg(16);
+    const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8;
+    b->fill_smem = cvg_fill_smem_bytes(dmax, N, tsz, 1, 1, 0, b->TS, pmax, b->block);
+    if (b->fill_smem > (size_t)ctx->smem_optin) {
+        delete b;
+        return cvg_internal_fail(CVG_ERR_INVALID, "batch: grid and histograms of the largest "
+                                                  "dimension do not fit shared memory");
+    }
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&b->arena, total);
+    if (e != cudaSuccess) {
+        delete b;
+        return cvg_internal_fail(CVG_ERR_NOMEM, std::string("batch arena: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    cudaStream_t st = ctx->stream;
+    BCK(cudaMemsetAsync(b->arena, 0, total, st));
+    char *ptr = (char *)b->arena;
+    auto take = [&](size_t bytes) { char *q = ptr; ptr += seg(bytes); return q; };
+    std::vector<cvg_fill_args> hf(n);
+    std::vector<cvg_realloc_args> hr(n);
+    std::vector<cvg_refine_args> hq(n);
+    std::vector<int> hdims(n);
+    std::vector<unsigned> blk_base(n + 1), dim_base(n + 1);
+    std::vector<double> xe;
+    b->d_status = (cvg_u32 *)take(16);
+    size_t th_off = 0;
+    for (int i = 0; i < n; ++i) {
+        inst_host &h = b->inst[i];
+        const int D = h.dim;
+        h.x_edges = (double *)take(sizeof(double) * D * (N + 1));
+        h.x_edges32 = (float *)take(sizeof(float) * D * (N + 1));
+        h.weights = (double *)take(sizeof(double) * D * N);
+        h.counts = (cvg_u32 *)take(sizeof(cvg_u32) * D * N);
+        h.JF = (double *)take(sizeof(double) * h.n_cubes);
+        h.JF2 = (double *)take(sizeof(double) * h.n_cubes);
+        h.dh = (double *)take(sizeof(double) * h.n_cubes);
+        h.nh_sum = (cvg_u64 *)take(sizeof(cvg_u64) * (h.n_cubes + 1ull));
+        h.nh_new = (cvg_u32 *)take(sizeof(cvg_u32) * h.n_cubes);
+        h.tile_cube = (cvg_u32 *)take(sizeof(cvg_u32) * h.max_tiles);
+        h.partials = (double *)take(sizeof(double) * 4 * h.nb);
+        h.bsums = (cvg_u64 *)take(sizeof(cvg_u64) * (h.nb + 1));
+        h.stats = (double *)take(sizeof(double) * 3 * p.max_it);
+        h.acc = (cvg_acc_dev *)take(sizeof(cvg_acc_dev));
+        h.iteration = (cvg_u32 *)take(16);
+        h.scale_exp = (int *)take(16);
+        take(16);
+        h.theta = (double *)take(sizeof(double) * std::max(1, h.n_params));
+        h.grad = (double *)take(sizeof(double) * std::max(1, h.n_params));
+        // uniform grid (src/main.cu:432-441)
+        xe.resize((size_t)D * (N + 1));
+        for (int d = 0; d < D; ++d)
+            for (int j = 0; j <= N; ++j) xe[(size_t)d * (N + 1) + j] = j * (1.0 / N);
+        BCK(cudaMemcpyAsync(h.x_edges, xe.data(), sizeof(double) * xe.size(), cudaMemcpyHostToDevice, st));
+        BCK(cvg_launch_grid32(h.x_edges, h.x_edges32, D * (N + 1), st));
+        if (h.n_params > 0 && theta)
+            BCK(cudaMemcpyAsync(h.theta, theta + th_off, sizeof(double) * h.n_params,
+                                cudaMemcpyHostToDevice, st));
+        th_off += h.n_params;
+        BCK(cvg_launch_fill_u32(h.nh_new, h.nh0, h.n_cubes, st));
+        BCK(cudaStreamSynchronize(st));   // xe is reused
+        cvg_fill_args &a = hf[i];
+        a.x_edges = h.x_edges;
+        a.x_edges32 = h.x_edges32;
+        a.nh_sum = h.nh_sum;
+        a.tile_cube = h.tile_cube;
+        a.iteration = h.iteration;
+        a.theta = h.theta;
+        a.JF = h.JF;
+        a.JF2 = h.JF2;
+        a.weights = h.weights;
+        a.counts = h.counts;
+        a.grad = h.grad;
+        a.status = b->d_status;
+        a.scale_exp = p.precision == CVG_PREC_FP32 ? h.scale_exp : nullptr;
+        a.max_tiles = h.max_tiles;
+        a.seed = p.seed;
+        a.instance = insts[i].instance;
+        a.n_cubes = h.n_cubes;
+        a.n_strat = h.n_strat;
+        a.n_intervals = N;
+        a.tile_samples = b->TS;
+        a.spt = b->spt;
+        a.n_params = h.n_params;
+        a.v_cubes = h.v_cubes;
+        cvg_realloc_args &r = hr[i];
+        r.nh_sum = h.nh_sum;
+        r.JF = h.JF;
+        r.JF2 = h.JF2;
+        r.dh = h.dh;
+        r.nh_new = h.nh_new;
+        r.partials = h.partials;
+        r.bsums = h.bsums;
+        r.tile_cube = h.tile_cube;
+        r.stats = h.stats;
+        r.acc = h.acc;
+        r.iteration = h.iteration;
+        r.status = b->d_status;
+        r.scale_exp = a.scale_exp;
+        r.max_tiles = h.max_tiles;
+        r.n_eval_it = h.n_eval_it;
+        r.v_cubes = h.v_cubes;
+        r.beta = p.beta;
+        r.n_cubes = h.n_cubes;
+        r.tile_samples = b->TS;
+        r.skip = p.skip;
+        r.max_it = p.max_it;
+        r.fast_pow = p.precision == CVG_PREC_FP32 ? 1 : 0;
+        r.adapt = (p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
+        cvg_refine_args &q = hq[i];
+        q.x_edges = h.x_edges;
+        q.x_edges32 = h.x_edges32;
+        q.weights = h.weights;
+        q.counts = h.counts;
+        q.alpha = p.alpha;
+        q.dim = D;
+        q.n_intervals = N;
+        q.adapt = r.adapt;
+        hdims[i] = D;
+        blk_base[i + 1] = blk_base[i] + h.nb;
+        dim_base[i + 1] = dim_base[i] + D;
+    }
+    b->total_blocks = blk_base[n];
+    b->total_dims = dim_base[n];
+    b->d_fill = (cvg_fill_args *)take(sizeof(cvg_fill_args) * n);
+    b->d_realloc = (cvg_realloc_args *)take(sizeof(cvg_realloc_args) * n);
+    b->d_refine = (cvg_refine_args *)take(sizeof(cvg_refine_args) * n);
+    b->d_dims = (int *)take(sizeof(int) * n);
+    b->d_blk_base = (unsigned *)take(sizeof(unsigned) * (n + 1));
+    b->d_dim_base = (unsigned *)take(sizeof(unsigned) * (n + 1));
+    b->d_tile_base = (cvg_u64 *)take(sizeof(cvg_u64) * (n + 1));
+    BCK(cudaMemcpyAsync(b->d_fill, hf.data(), sizeof(cvg_fill_args) * n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_realloc, hr.data(), sizeof(cvg_realloc_args) * n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_refine, hq.data(), sizeof(cvg_refine_args) * n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_dims, hdims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_blk_base, blk_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_dim_base, dim_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
+    // initial counts -> prefixes, tile maps, tile numbering
+    BCK(cvg_launch_set_nh_batch(realloc_batch(b), b->d_tile_base, st));
+    // kernels
+    cudaLibrary_t lib = nullptr;
+    BCKS(cvg_internal_load_module(ctx, batch_source(*b, dims), &lib));
+    BCK(cudaLibraryGetKernel(&b->fill, lib, "cvg_fill_batch_entry"));
+    BCK(cudaLibraryGetKernel(&b->pilot, lib, "cvg_pilot_batch_entry"));
+    BCK(cudaFuncSetAttribute((const void *)b->fill, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)b->fill_smem));
+    int occ = 0;
+    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)b->fill, b->block, b->fill_smem));
+    if (occ < 1) return cvg_internal_fail(CVG_ERR_INVALID, "batched fill kernel cannot be resident");
+    b->grid = occ * ctx->n_sm;
+    BCK(cudaEventCreate(&b->ev0));
+    BCK(cudaEventCreate(&b->ev1));
+    // FP32 form: per-instance scale exponent from a pilot evaluation
+    if (p.precision == CVG_PREC_FP32) {
+        std::vector<int> ex(n, -1000);
+        for (int i = 0; i < n; ++i)
+            BCK(cudaMemcpyAsync(b->inst[i].scale_exp, &ex[i], sizeof(int), cudaMemcpyHostToDevice, st));
+        cvg_batch_args ba = batch_args(b);
+        void *args[] = {&ba};
+        BCK(cudaLaunchKernel((const void *)b->pilot, dim3(8 * n), dim3(256), args, 0, st));
+        for (int i = 0; i < n; ++i)
+            BCK(cudaMemcpyAsync(&ex[i], b->inst[i].scale_exp, sizeof(int), cudaMemcpyDeviceToHost, st));
+        BCK(cudaStreamSynchronize(st));
+        for (int i = 0; i < n; ++i) {
+            ex[i] = ex[i] < -100 ? 0 : std::min(ex[i], 100);
+            BCK(cudaMemcpyAsync(b->inst[i].scale_exp, &ex[i], sizeof(int), cudaMemcpyHostToDevice, st));
+        }
+    }
+    BCK(cudaStreamSynchronize(st));
+    return CVG_OK;
+}
+
+cvg_status cvg_batch_destroy(cvg_batch b)
+{
+    if (!b) return CVG_OK;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->arena) cudaFree(b->arena);
+    delete b;
+    return CVG_OK;
+}
+
+cvg_status cvg_batch_iterate(cvg_batch b, int32_t n_it)
+{
+    if (!b) return cvg_internal_fail(CVG_ERR_INVALID, "NULL batch");
+    if (n_it < 0 || b->it_done + n_it > b->p.max_it)
+        return cvg_internal_fail(CVG_ERR_STATE, "iterations beyond max_it");
+    BCK(cudaSetDevice(b->ctx->device));
+    if (b->p.flags & CVG_FLAG_GRAPH) {
+        if (!b->graph_exec) {
+            cudaStream_t s = b->ctx->stream;
+            BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            cvg_status st = enqueue_iteration(b, false);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (st != CVG_OK) { if (g) cudaGraphDestroy(g); return st; }
+            BCK(e);
+            b->graph = g;
+            BCK(cudaGraphInstantiate(&b->graph_exec, g, 0));
+        }
+        for (int i = 0; i < n_it; ++i) BCK(cudaGraphLaunch(b->graph_exec, b->ctx->stream));
+    } else {
+        for (int i = 0; i < n_it; ++i) BCKS(enqueue_iteration(b, i == n_it - 1));
+    }
+    b->it_done += n_it;
+    return CVG_OK;
+}
+
+cvg_status cvg_batch_results(cvg_batch b, cvg_result *out, double *it_res, double *it_sig2)
+{
+    if (!b || !out) return cvg_internal_fail(CVG_ERR_INVALID, "NULL argument");
+    BCK(cudaSetDevice(b->ctx->device));
+    const int M = b->p.max_it;
+    std::vector<double> stats((size_t)3 * M * b->n);
+    std::vector<cvg_acc_dev> acc(b->n);
+    cvg_u32 status = 0;
+    cudaStream_t st = b->ctx->stream;
+    for (int i = 0; i < b->n; ++i) {
+        BCK(cudaMemcpyAsync(stats.data() + (size_t)3 * M * i, b->inst[i].stats, sizeof(double) * 3 * M,
+                            cudaMemcpyDeviceToHost, st));
+        BCK(cudaMemcpyAsync(&acc[i], b->inst[i].acc, sizeof(cvg_acc_dev), cudaMemcpyDeviceToHost, st));
+    }
+    BCK(cudaMemcpyAsync(&status, b->d_status, sizeof(status), cudaMemcpyDeviceToHost, st));
+    BCK(cudaStreamSynchronize(st));
+    if (status & CVG_KSTAT_BAD_TILE)
+        return cvg_internal_fail(CVG_ERR_KERNEL, "batched fill found an inconsistent tile map");
+    const int done = std::min(b->it_done, M);
+    for (int i = 0; i < b->n; ++i) {
+        cvg_result &r = out[i];
+        std::memset(&r, 0, sizeof(r));
+        const double *s = stats.data() + (size_t)3 * M * i;
+        cvg_internal_result(s, M, done, b->p.skip, &r);
+        r.n_strat = b->inst[i].n_strat;
+        r.n_intervals = b->p.n_intervals;
+        r.n_cubes = b->inst[i].n_cubes;
+        r.tot_nevals = (int64_t)acc[i].tot_nevals;
+        r.seed = b->p.seed;
+        r.gpu_thr = b->p.gpu_thr;
+        r.precision = b->p.precision;
+        if (it_res) for (int k = 0; k < M; ++k) it_res[(size_t)i * M + k] = s[k];
+        if (it_sig2) for (int k = 0; k < M; ++k) it_sig2[(size_t)i * M + k] = s[M + k];
+    }
+    return CVG_OK;
+}
+
+cvg_status cvg_batch_info_get(cvg_batch b, int32_t *block, int32_t *spt, int32_t *grid,
+                              int64_t *fill_smem_bytes, int64_t *next_samples)
+{
+    if (!b) return cvg_internal_fail(CVG_ERR_INVALID, "NULL batch");
+    if (block) *block = b->block;
+    if (spt) *spt = b->spt;
+    if (grid) *grid = b->grid;
+    if (fill_smem_bytes) *fill_smem_bytes = (int64_t)b->fill_smem;
+    if (next_samples) {
+        BCK(cudaSetDevice(b->ctx->device));
+        int64_t tot = 0;
+        for (int i = 0; i < b->n; ++i) {
+            cvg_u64 S = 0;
+            BCK(cudaMemcpyAsync(&S, b->inst[i].nh_sum + b->inst[i].n_cubes, sizeof(S),
+                                cudaMemcpyDeviceToHost, b->ctx->stream));
+            BCK(cudaStreamSynchronize(b->ctx->stream));
+            tot += (int64_t)S;
+        }
+        *next_samples = tot;
+    }
+    return CVG_OK;
+}
+
+cvg_status cvg_batch_compile_check(const char *source, int32_t n_dims, const int32_t *dims,
+                                   const int32_t *params_per_dim, int32_t precision,
+                                   int32_t block, const char *arch, char *log, size_t log_len)
+{
+    if (!source || !dims || !params_per_dim || !arch || n_dims < 1)
+        return cvg_internal_fail(CVG_ERR_INVALID, "NULL argument");
+    cvg_batch_s b;
+    b.f.source = source;
+    b.f.abi = CVG_ABI_NATIVE;
+    b.p.precision = precision;
+    b.block = block > 0 ? block : 512;
+    b.params_per_dim.assign(params_per_dim, params_per_dim + 17);
+    std::set<int> ds;
+    for (int i = 0; i < n_dims; ++i) {
+        if (dims[i] < 1 || dims[i] > 16) return cvg_internal_fail(CVG_ERR_INVALID, "dims in [1, 16]");
+        ds.insert(dims[i]);
+    }
+    std::string l;
+    const cvg_status st = cvg_internal_compile_only(batch_source(b, ds), arch, l);
+    if (log && log_len) {
+        std::strncpy(log, l.c_str(), log_len - 1);
+        log[log_len - 1] = '\0';
+    }
+    return st;
+}
+
+cvg_status cvg_batch_last_fill_ms(cvg_batch b, float *ms)
+{
+    if (!b || !ms) return cvg_internal_fail(CVG_ERR_INVALID, "NULL argument");
+    BCK(cudaEventSynchronize(b->ev1));
+    BCK(cudaEventElapsedTime(ms, b->ev0, b->ev1));
+    return CVG_OK;
+}
+
+}  // extern "C"

@@ -49,6 +49,14 @@ struct cvg_fill_args {
     double v_cubes;               // volume of one hypercube
 };
 
+// Arguments of one batched fill launch.
+struct cvg_batch_args {
+    const cvg_fill_args *inst;    // [n_inst]
+    const int *dims;              // [n_inst]
+    const cvg_u64 *tile_base;     // [n_inst + 1] first global tile of each instance
+    int n_inst;
+};
+
 CVG_HD cvg_u64 cvg_align16(cvg_u64 x) { return (x + 15ull) & ~15ull; }
 
 // Dynamic shared memory of one fill launch; the kernel carves it in the same

@@ -23,9 +23,9 @@
 // without float/int conversions and run sums are widened to FP64 by bit
 // splicing before the (L2-executed) FP64 atomics.
 //
-// Expects, before inclusion: cvg_common.cuh, and the macros
-//   CVG_F(x, th)          -> integrand value at x (T* x, const T* th)
-//   CVG_DF(x, th, g)      -> gradient w.r.t. theta into g[] (gradient pass only)
+// Expects cvg_common.cuh before inclusion.  The integrand comes in as a type
+// F with static members  T f(T* x, const T* th)  and
+// void df(T* x, const T* th, T* g)  (gradient w.r.t. theta; gradient pass).
 #ifndef CVG_FILL_CUH
 #define CVG_FILL_CUH
 
@@ -144,13 +144,246 @@ CVG_D void cvg_cube_next(int ns, T dy, int *coord, T *cdy)
     }
 }
 
-template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD>
+// Shared-memory views of one fill CTA, carved in the order of
+// cvg_fill_smem_bytes: theta | bin sums | grid | bin counts | cube starts | scratch.
+template <int D, typename T, bool ESM, bool HSM, int P, bool GRAD>
+struct cvg_fill_smem {
+    T *th, *hw, *E;
+    cvg_u32 *hc;
+    int *starts;
+    double *red;
+    CVG_D void carve(unsigned char *base, int N, int TS)
+    {
+        constexpr bool H = HSM && !GRAD;
+        cvg_u64 off = 0;
+        th = (T *)(base + off);
+        off += cvg_align16((cvg_u64)P * sizeof(T));
+        hw = (T *)(base + off);
+        if (H) off += cvg_align16((cvg_u64)D * N * sizeof(T));
+        E = (T *)(base + off);
+        if (ESM) off += cvg_align16((cvg_u64)D * (N + 1) * sizeof(T));
+        hc = (cvg_u32 *)(base + off);
+        if (H) off += cvg_align16((cvg_u64)D * N * 4);
+        starts = (int *)(base + off);
+        off += cvg_align16((cvg_u64)(TS / 2 + 4) * 4);
+        red = (double *)(base + off);
+    }
+};
+
+// Per-instance constants of a fill CTA.
+template <typename T>
+struct cvg_fill_ctx {
+    const T *G;
+    cvg_u32 it, k0, k1, c3;
+    int ns, N, kx;
+    T dy, fN, fNm1, vc, jac0;
+};
+
+// Load theta and the grid into shared memory, clear the bin histograms and
+// set the per-instance constants.  The caller synchronises afterwards.
+template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD>
+CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
+                          cvg_fill_ctx<T> &cx)
+{
+    constexpr bool H = HSM && !GRAD;
+    const int N = a.n_intervals, tid = threadIdx.x;
+    const T *grid = cvg_grid_src<T>::get(a);
+    if (P > 0)
+        for (int i = tid; i < P; i += BS) sm.th[i] = (T)a.theta[i];
+    if (ESM)
+        for (int i = tid; i < D * (N + 1); i += BS) sm.E[i] = grid[i];
+    if (H)
+        for (int i = tid; i < D * N; i += BS) { sm.hw[i] = (T)0; sm.hc[i] = 0u; }
+    cx.G = ESM ? sm.E : grid;
+    cx.it = *a.iteration;
+    cx.k0 = (cvg_u32)a.seed;
+    cx.k1 = (cvg_u32)(a.seed >> 32);
+    cx.c3 = a.instance << 8;
+    cx.ns = a.n_strat;
+    cx.N = N;
+    cx.dy = (T)1 / (T)a.n_strat;
+    cx.fN = (T)N;
+    cx.fNm1 = (T)(N - 1);
+    cx.vc = (T)a.v_cubes;
+    // FP32 form: f*jac is carried as f*jac*2^-k so its square stays in range;
+    // sums are widened back with the exponent shift (exact)
+    cx.kx = (sizeof(T) == 4 && a.scale_exp) ? *a.scale_exp : 0;
+    cx.jac0 = cvg_scale_pow2((T)0, cx.kx);
+}
+
+// One tile: samples [tile*TS, min((tile+1)*TS, S)).  Returns false (and sets a
+// status bit) if the tile map is inconsistent; uniform across the block.
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F>
+CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
+                         const cvg_fill_ctx<T> &cx, cvg_u64 tile, cvg_u64 n_tiles, cvg_u64 S,
+                         cvg_acc<T> *gacc)
+{
+    constexpr int PP = P > 0 ? P : 1;
+    constexpr int NB = (D + 3) / 4;
+    constexpr bool H = HSM && !GRAD;
+    const int tid = threadIdx.x;
+    const int TS = a.tile_samples, N = cx.N, ns = cx.ns;
+    const T dy = cx.dy, fN = cx.fN, fNm1 = cx.fNm1;
+    const T *G = cx.G;
+    int *starts = sm.starts;
+    const cvg_u64 base = tile * (cvg_u64)TS;
+    const cvg_u32 c_lo = a.tile_cube[tile];
+    const cvg_u32 c_hi = (tile + 1 < n_tiles) ? a.tile_cube[tile + 1] : a.n_cubes - 1;
+    if (c_hi < c_lo || c_hi >= a.n_cubes || (int)(c_hi - c_lo) > TS / 2 + 1) {
+        if (tid == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
+        return false;
+    }
+    const int K = (int)(c_hi - c_lo) + 2;
+    for (int i = tid; i < K; i += BS)
+        starts[i] = (int)((cvg_i64)a.nh_sum[c_lo + i] - (cvg_i64)base);
+    __syncthreads();
+
+    const int spt = a.spt;
+    const int l0 = tid * spt;
+    const cvg_u64 rem = S - base;
+    const int lend_tile = rem < (cvg_u64)TS ? (int)rem : TS;
+    if (l0 < lend_tile) {
+        int lo = 0, hi = K - 2;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (starts[mid] <= l0) lo = mid; else hi = mid - 1;
+        }
+        int ci = lo;
+        cvg_u32 c = c_lo + (cvg_u32)ci;
+        int cstart = starts[ci];
+        int next = starts[ci + 1];
+        cvg_u32 j = (cvg_u32)(l0 - cstart);
+        int coord[D];
+        T cdy[D];
+        cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
+        const int lend = min(l0 + spt, lend_tile);
+
+        cvg_acc<T> a1, a2;
+        a1.reset(); a2.reset();
+        T ag[PP];
+#pragma unroll
+        for (int p = 0; p < PP; ++p) ag[p] = (T)0;
+        int run = 0;   // samples in the current cube run
+
+        for (int l = l0; l < lend; ++l) {
+            if (l >= next) {
+                // run [max(cstart, l0), next) is complete: private to this
+                // thread unless its cube began before l0
+                if (run > 0) {
+                    if (GRAD) {
+                        const T sc = cx.vc / (T)(next - cstart);
+#pragma unroll
+                        for (int p = 0; p < PP; ++p) { gacc[p].add(ag[p] * sc); ag[p] = (T)0; }
+                    } else {
+                        const double v1 = cvg_to_double_scaled(a1.value_t(), cx.kx);
+                        const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * cx.kx);
+                        if (cstart >= l0) { a.JF[c] = v1; a.JF2[c] = v2; }
+                        else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
+                        a1.reset(); a2.reset();
+                    }
+                    run = 0;
+                }
+                do {  // empty cubes (never produced by the reallocation) are skipped
+                    ++ci; ++c;
+                    cvg_cube_next<D, T>(ns, dy, coord, cdy);
+                    cstart = next;
+                    next = starts[ci + 1];
+                } while (l >= next && ci < K - 2);
+                j = 0u;
+            }
+            ++run;
+            cvg_u32 rr[NB * 4];
+            if (!REPLAY) {
+#pragma unroll
+                for (int b = 0; b < NB; ++b) {
+                    const cvg_u32x4 r4 = cvg_philox(j, c, cx.it, (cvg_u32)b | cx.c3, cx.k0, cx.k1);
+                    rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y;
+                    rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
+                }
+            }
+            T x[D];
+            int bin[D];
+            T jac = cx.jac0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                T u;
+                if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
+                else u = cvg_uniform<T>(rr[d]);
+                const T y = cvg_fma(u, dy, cdy[d]);
+                const T z = y * fN;
+                T frac;
+                const int b = cvg_bin(z, N, fNm1, frac);
+                const T e0 = G[d * (N + 1) + b];
+                const T e1 = G[d * (N + 1) + b + 1];
+                const T dx = e1 - e0;
+                x[d] = cvg_fma(dx, frac, e0);
+                jac *= fN * dx;
+                bin[d] = b;
+            }
+            if (GRAD) {
+                T g[PP];
+                F::df(x, sm.th, g);
+#pragma unroll
+                for (int p = 0; p < PP; ++p) ag[p] += g[p] * jac;
+            } else {
+                const T jf = (T)F::f(x, sm.th) * jac;
+                const T jf2 = jf * jf;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    if (H) {
+                        atomicAdd(&sm.hw[d * N + bin[d]], jf2);
+                        atomicAdd(&sm.hc[d * N + bin[d]], 1u);
+                    } else {
+                        atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
+                        atomicAdd(&a.counts[d * N + bin[d]], 1u);
+                    }
+                }
+                a1.add(jf);
+                a2.add(jf2);
+            }
+            ++j;
+        }
+        if (run > 0) {   // last run: private only if it began here and its cube ends here
+            if (GRAD) {
+                const T sc = cx.vc / (T)(next - cstart);
+#pragma unroll
+                for (int p = 0; p < PP; ++p) gacc[p].add(ag[p] * sc);
+            } else {
+                const double v1 = cvg_to_double_scaled(a1.value_t(), cx.kx);
+                const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * cx.kx);
+                if (cstart >= l0 && next == lend) { a.JF[c] = v1; a.JF2[c] = v2; }
+                else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
+            }
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// Add the CTA's shared-memory bin histograms to the global FP64/u32 ones.
+template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD>
+CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm)
+{
+    if (!(HSM && !GRAD)) return;
+    __syncthreads();
+    const int N = a.n_intervals;
+    for (int i = threadIdx.x; i < D * N; i += BS) {
+        const cvg_u32 cn = sm.hc[i];
+        if (cn) {
+            atomicAdd(&a.weights[i], cvg_to_double(sm.hw[i]));
+            atomicAdd(&a.counts[i], cn);
+        }
+    }
+    __syncthreads();
+}
+
+// Persistent single-instance fill: this CTA takes tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F>
 CVG_D void cvg_fill_body(const cvg_fill_args &a)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
     constexpr int PP = P > 0 ? P : 1;
-    constexpr int NB = (D + 3) / 4;
-    const int N = a.n_intervals;
     const int tid = threadIdx.x;
     const cvg_u64 S = a.nh_sum[a.n_cubes];
     const int TS = a.tile_samples;
@@ -161,210 +394,87 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     }
     if ((cvg_u64)blockIdx.x >= n_tiles) return;
 
-    // ---- shared memory carve (same order as cvg_fill_smem_bytes) ----
-    constexpr bool H = HSM && !GRAD;
-    cvg_u64 off = 0;
-    T *th = (T *)(cvg_smem + off);
-    off += cvg_align16((cvg_u64)P * sizeof(T));
-    T *hw = (T *)(cvg_smem + off);
-    if (H) off += cvg_align16((cvg_u64)D * N * sizeof(T));
-    T *E = (T *)(cvg_smem + off);
-    if (ESM) off += cvg_align16((cvg_u64)D * (N + 1) * sizeof(T));
-    cvg_u32 *hc = (cvg_u32 *)(cvg_smem + off);
-    if (H) off += cvg_align16((cvg_u64)D * N * 4);
-    int *starts = (int *)(cvg_smem + off);
-    off += cvg_align16((cvg_u64)(TS / 2 + 4) * 4);
-    double *red = (double *)(cvg_smem + off);
-
-    const T *grid = cvg_grid_src<T>::get(a);
-    if (P > 0)
-        for (int i = tid; i < P; i += BS) th[i] = (T)a.theta[i];
-    if (ESM)
-        for (int i = tid; i < D * (N + 1); i += BS) E[i] = grid[i];
-    if (H)
-        for (int i = tid; i < D * N; i += BS) { hw[i] = (T)0; hc[i] = 0u; }
-
-    const cvg_u32 it = *a.iteration;
-    const cvg_u32 k0 = (cvg_u32)a.seed, k1 = (cvg_u32)(a.seed >> 32);
-    const cvg_u32 c3 = a.instance << 8;
-    const int ns = a.n_strat;
-    const T dy = (T)1 / (T)ns;
-    const T fN = (T)N;
-    const T fNm1 = (T)(N - 1);
-    const T *G = ESM ? E : grid;
-    const T vc = (T)a.v_cubes;
-    // FP32 form: f*jac is carried as f*jac*2^-k so its square stays in range;
-    // sums are widened back with the exponent shift (exact)
-    const int kx = (sizeof(T) == 4 && a.scale_exp) ? *a.scale_exp : 0;
-    const T jac0 = cvg_scale_pow2((T)0, kx);
-
+    cvg_fill_smem<D, T, ESM, HSM, P, GRAD> sm;
+    sm.carve(cvg_smem, a.n_intervals, TS);
+    cvg_fill_ctx<T> cx;
+    cvg_fill_setup<D, T, BS, ESM, HSM, P, GRAD>(a, sm, cx);
     cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
 #pragma unroll
     for (int p = 0; p < PP; ++p) gacc[p].reset();
-
     __syncthreads();
 
-    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        const cvg_u64 base = tile * (cvg_u64)TS;
-        const cvg_u32 c_lo = a.tile_cube[tile];
-        const cvg_u32 c_hi = (tile + 1 < n_tiles) ? a.tile_cube[tile + 1] : a.n_cubes - 1;
-        if (c_hi < c_lo || c_hi >= a.n_cubes || (int)(c_hi - c_lo) > TS / 2 + 1) {
-            if (tid == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
-            break;  // uniform across the block
-        }
-        const int K = (int)(c_hi - c_lo) + 2;
-        for (int i = tid; i < K; i += BS)
-            starts[i] = (int)((cvg_i64)a.nh_sum[c_lo + i] - (cvg_i64)base);
-        __syncthreads();
+    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F>(a, sm, cx, tile, n_tiles, S, gacc))
+            break;
 
-        const int spt = a.spt;
-        const int l0 = tid * spt;
-        const cvg_u64 rem = S - base;
-        const int lend_tile = rem < (cvg_u64)TS ? (int)rem : TS;
-        if (l0 < lend_tile) {
-            int lo = 0, hi = K - 2;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (starts[mid] <= l0) lo = mid; else hi = mid - 1;
-            }
-            int ci = lo;
-            cvg_u32 c = c_lo + (cvg_u32)ci;
-            int cstart = starts[ci];
-            int next = starts[ci + 1];
-            cvg_u32 j = (cvg_u32)(l0 - cstart);
-            int coord[D];
-            T cdy[D];
-            cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
-            const int lend = min(l0 + spt, lend_tile);
-
-            cvg_acc<T> a1, a2;
-            a1.reset(); a2.reset();
-            T ag[PP];
-#pragma unroll
-            for (int p = 0; p < PP; ++p) ag[p] = (T)0;
-            int run = 0;   // samples in the current cube run
-
-            for (int l = l0; l < lend; ++l) {
-                if (l >= next) {
-                    // run [max(cstart, l0), next) is complete: private to this
-                    // thread unless its cube began before l0
-                    if (run > 0) {
-                        if (GRAD) {
-                            const T sc = vc / (T)(next - cstart);
-#pragma unroll
-                            for (int p = 0; p < PP; ++p) { gacc[p].add(ag[p] * sc); ag[p] = (T)0; }
-                        } else {
-                            const double v1 = cvg_to_double_scaled(a1.value_t(), kx);
-                            const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * kx);
-                            if (cstart >= l0) { a.JF[c] = v1; a.JF2[c] = v2; }
-                            else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
-                            a1.reset(); a2.reset();
-                        }
-                        run = 0;
-                    }
-                    do {  // empty cubes (never produced by the reallocation) are skipped
-                        ++ci; ++c;
-                        cvg_cube_next<D, T>(ns, dy, coord, cdy);
-                        cstart = next;
-                        next = starts[ci + 1];
-                    } while (l >= next && ci < K - 2);
-                    j = 0u;
-                }
-                ++run;
-                cvg_u32 rr[NB * 4];
-                if (!REPLAY) {
-#pragma unroll
-                    for (int b = 0; b < NB; ++b) {
-                        const cvg_u32x4 r4 = cvg_philox(j, c, it, (cvg_u32)b | c3, k0, k1);
-                        rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y;
-                        rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
-                    }
-                }
-                T x[D];
-                int bin[D];
-                T jac = jac0;
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    T u;
-                    if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
-                    else u = cvg_uniform<T>(rr[d]);
-                    const T y = cvg_fma(u, dy, cdy[d]);
-                    const T z = y * fN;
-                    T frac;
-                    const int b = cvg_bin(z, N, fNm1, frac);
-                    const T e0 = G[d * (N + 1) + b];
-                    const T e1 = G[d * (N + 1) + b + 1];
-                    const T dx = e1 - e0;
-                    x[d] = cvg_fma(dx, frac, e0);
-                    jac *= fN * dx;
-                    bin[d] = b;
-                }
-                if (GRAD) {
-#if defined(CVG_HAS_GRAD)
-                    T g[PP];
-                    CVG_DF(x, th, g);
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) ag[p] += g[p] * jac;
-#endif
-                } else {
-                    const T jf = (T)CVG_F(x, th) * jac;
-                    const T jf2 = jf * jf;
-#pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        if (H) {
-                            atomicAdd(&hw[d * N + bin[d]], jf2);
-                            atomicAdd(&hc[d * N + bin[d]], 1u);
-                        } else {
-                            atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
-                            atomicAdd(&a.counts[d * N + bin[d]], 1u);
-                        }
-                    }
-                    a1.add(jf);
-                    a2.add(jf2);
-                }
-                ++j;
-            }
-            if (run > 0) {   // last run: private only if it began here and its cube ends here
-                if (GRAD) {
-                    const T sc = vc / (T)(next - cstart);
-#pragma unroll
-                    for (int p = 0; p < PP; ++p) gacc[p].add(ag[p] * sc);
-                } else {
-                    const double v1 = cvg_to_double_scaled(a1.value_t(), kx);
-                    const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * kx);
-                    if (cstart >= l0 && next == lend) { a.JF[c] = v1; a.JF2[c] = v2; }
-                    else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
-                }
-            }
-        }
-        __syncthreads();
-    }
-
-    if (H) {
-        __syncthreads();
-        for (int i = tid; i < D * N; i += BS) {
-            const cvg_u32 cn = hc[i];
-            if (cn) {
-                atomicAdd(&a.weights[i], cvg_to_double(hw[i]));
-                atomicAdd(&a.counts[i], cn);
-            }
-        }
-    }
+    cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD>(a, sm);
     if (GRAD) {
         const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
         for (int p = 0; p < PP; ++p) {
-            double v = ldexp(gacc[p].value(), kx);
+            double v = ldexp(gacc[p].value(), cx.kx);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) red[warp * PP + p] = v;
+            if (lane == 0) sm.red[warp * PP + p] = v;
         }
         __syncthreads();
         if (tid < PP && tid < P) {
             double v = 0.0;
-            for (int w = 0; w < BS / 32; ++w) v += red[w * PP + tid];
+            for (int w = 0; w < BS / 32; ++w) v += sm.red[w * PP + tid];
             atomicAdd(&a.grad[tid], v);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched fill: many independent integrals (different dimensions and sample
+// counts) in one persistent launch.  Tiles of all instances are numbered
+// globally (tile_base[i] = first tile of instance i this iteration); CTA b
+// takes a contiguous range of tiles, so it meets few instance changes.  On a
+// change it flushes the previous instance's histograms and loads the next
+// instance's grid.  DISP::run(dim, op) calls op(cvg_int<D>, cvg_int<P>) for
+// the dimensions present; DISP::fn<D> is the integrand of dimension D.
+// ---------------------------------------------------------------------------
+template <int V> struct cvg_int { static constexpr int value = V; };
+
+
+template <typename T, int BS, class DISP>
+CVG_D void cvg_fill_batch(const cvg_batch_args &b)
+{
+    extern __shared__ __align__(16) unsigned char cvg_smem[];
+    const cvg_u64 total = b.tile_base[b.n_inst];
+    const cvg_u64 chunk = (total + gridDim.x - 1) / gridDim.x;
+    cvg_u64 t = (cvg_u64)blockIdx.x * chunk;
+    const cvg_u64 t1 = min(t + chunk, total);
+    if (t >= t1) return;
+    int lo = 0, hi = b.n_inst - 1;            // instance holding tile t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b.tile_base[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    int i = lo;
+    while (t < t1) {
+        while (b.tile_base[i + 1] <= t) ++i;   // skip instances without tiles
+        const cvg_u64 tb = b.tile_base[i];
+        const cvg_u64 te = min(t1, b.tile_base[i + 1]);
+        const cvg_fill_args a = b.inst[i];
+        DISP::run(b.dims[i], [&](auto Dc, auto Pc) {
+            constexpr int D = decltype(Dc)::value, P = decltype(Pc)::value;
+            using F = typename DISP::template fn<D>;
+            cvg_fill_smem<D, T, true, true, P, false> sm;
+            sm.carve(cvg_smem, a.n_intervals, a.tile_samples);
+            cvg_fill_ctx<T> cx;
+            cvg_fill_setup<D, T, BS, true, true, P, false>(a, sm, cx);
+            __syncthreads();
+            const cvg_u64 S = a.nh_sum[a.n_cubes];
+            const cvg_u64 nt = b.tile_base[i + 1] - tb;
+            for (cvg_u64 lt = t - tb; lt < te - tb; ++lt)
+                if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F>(a, sm, cx, lt, nt, S,
+                                                                             nullptr))
+                    break;
+            cvg_fill_flush<D, T, BS, true, true, P, false>(a, sm);
+        });
+        t = te;
     }
 }
 
@@ -372,13 +482,13 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 // one sample in each of the first cubes (grid as it is now, Philox counter
 // word 2 = 0xFFFFFFFF so no iteration's samples are reused).  Results are
 // combined with atomicMax into *a.scale_exp (initialised by the host).
-template <int D, typename T, int BS, int P>
-CVG_D void cvg_pilot_body(const cvg_fill_args &a)
+template <int D, typename T, int BS, int P, class F>
+CVG_D void cvg_pilot_body(const cvg_fill_args &a, cvg_u32 blk)
 {
     __shared__ T th[P > 0 ? P : 1];
     for (int i = threadIdx.x; i < P; i += BS) th[i] = (T)a.theta[i];
     __syncthreads();
-    const cvg_u32 gid = blockIdx.x * BS + threadIdx.x;
+    const cvg_u32 gid = blk * BS + threadIdx.x;
     const cvg_u32 c = gid % a.n_cubes;
     const cvg_u32 j = gid / a.n_cubes;
     const int N = a.n_intervals, ns = a.n_strat;
@@ -407,7 +517,7 @@ CVG_D void cvg_pilot_body(const cvg_fill_args &a)
         x[d] = cvg_fma(dx, frac, e0);
         jac *= fN * dx;
     }
-    const T v = (T)CVG_F(x, th) * jac;
+    const T v = (T)F::f(x, th) * jac;
     const float fv = fabsf((float)v);
     int e = -200;
     if (fv > 0.f && fv <= 3.4e38f) e = (int)((__float_as_uint(fv) >> 23) & 0xFFu) - 127;
@@ -415,6 +525,19 @@ CVG_D void cvg_pilot_body(const cvg_fill_args &a)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, o));
     if ((threadIdx.x & 31) == 0) atomicMax(a.scale_exp, e);
+}
+
+// Batched pilot: blocks [i*PB, (i+1)*PB) evaluate instance i.
+template <typename T, int PB, class DISP>
+CVG_D void cvg_pilot_batch(const cvg_batch_args &b)
+{
+    const int i = blockIdx.x / PB;
+    if (i >= b.n_inst) return;
+    const cvg_fill_args a = b.inst[i];
+    DISP::run(b.dims[i], [&](auto Dc, auto Pc) {
+        constexpr int D = decltype(Dc)::value, P = decltype(Pc)::value;
+        cvg_pilot_body<D, T, 256, P, typename DISP::template fn<D>>(a, blockIdx.x % PB);
+    });
 }
 
 #endif  // CVG_FILL_CUH

@@ -75,23 +75,7 @@ uint64_t fnv1a(const std::string &s, uint64_t h = 1469598103934665603ull)
 
 void cvg_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
 
-struct cvg_context_s {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int n_sm = 0;
-    int smem_optin = 0;
-    int cc_major = 0, cc_minor = 0;
-    std::string arch;
-    std::mutex mu;
-    std::unordered_map<uint64_t, cudaLibrary_t> libs;
-};
-
-struct cvg_integrand_s {
-    cvg_context ctx = nullptr;
-    std::string source;
-    int dim = 0, abi = 0, n_params = 0, has_grad = 0;
-};
+#include "cvg_internal.h"
 
 struct fill_variant {
     cudaKernel_t kernel = nullptr;
@@ -184,6 +168,29 @@ struct variant_key {
     int dim, prec, block, esm, hsm, replay, n_params, grad, abi;
 };
 
+// Integrand adaptor type F of the fill templates: static f (value) and df
+// (gradient w.r.t. theta) forwarding to the user's `integrand` /
+// `integrand_grad`, qualified by `ns` (a namespace prefix, or "").
+std::string fn_struct(const char *name, const cvg_integrand_s &f, int abi, int n_params, int grad,
+                      const std::string &ns)
+{
+    std::string s = std::string("struct ") + name + " {\n";
+    s += "  template <class T> static __device__ __forceinline__ T f(T* x, const T* th) {\n";
+    if (abi == CVG_ABI_NUMBA)
+        s += "    (void)th; double r = 0.0; " + ns + "integrand(&r, x); return r;\n";
+    else if (n_params > 0)
+        s += "    return " + ns + "integrand(x, th);\n";
+    else
+        s += "    (void)th; return " + ns + "integrand(x);\n";
+    s += "  }\n";
+    s += "  template <class T> static __device__ __forceinline__ void df(T* x, const T* th, T* g) {\n";
+    if (grad) s += "    " + ns + "integrand_grad(x, th, g);\n";
+    else s += "    (void)x; (void)th; (void)g;\n";
+    s += "  }\n};\n";
+    (void)f;
+    return s;
+}
+
 std::string make_source(const cvg_integrand_s &f, const variant_key &k)
 {
     const char *T = k.prec == CVG_PREC_FP32 ? "float" : "double";
@@ -194,25 +201,14 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     s += "#line 1 \"integrand.cu\"\n";
     s += f.source;
     s += "\n#line 1 \"cvg_adaptor\"\n";
-    if (k.abi == CVG_ABI_NUMBA) {
-        s += "__device__ __forceinline__ double cvg_numba_call(double* x) { double r = 0.0; "
-             "integrand(&r, x); return r; }\n";
-        s += "#define CVG_F(x, th) cvg_numba_call(x)\n";
-    } else if (k.n_params > 0) {
-        s += "#define CVG_F(x, th) integrand(x, th)\n";
-    } else {
-        s += "#define CVG_F(x, th) integrand(x)\n";
-    }
-    if (k.grad) {
-        s += "#define CVG_HAS_GRAD 1\n#define CVG_DF(x, th, g) integrand_grad(x, th, g)\n";
-    }
     s += cvg_src_fill;
+    s += fn_struct("cvg_fn_user", f, k.abi, k.n_params, k.grad, "");
     char entry[1024];
     std::snprintf(entry, sizeof(entry),
                   "\nextern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_entry("
-                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s>(a); }\n"
+                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s, cvg_fn_user>(a); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_entry("
-                  "const cvg_fill_args a) { cvg_pilot_body<%d, %s, 256, %d>(a); }\n",
+                  "const cvg_fill_args a) { cvg_pilot_body<%d, %s, 256, %d, cvg_fn_user>(a, blockIdx.x); }\n",
                   k.block, k.dim, T, k.block, k.esm ? "true" : "false",
                   k.hsm ? "true" : "false", k.replay ? "true" : "false", k.n_params,
                   k.grad ? "true" : "false", k.dim, T, k.n_params);
@@ -255,10 +251,8 @@ std::vector<std::string> nvrtc_options(const std::string &arch)
     return o;
 }
 
-cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_key &k,
-                      cudaKernel_t *out, cudaKernel_t *pilot = nullptr)
+cvg_status load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *out)
 {
-    const std::string src = make_source(f, k);
     const std::vector<std::string> opts = nvrtc_options(ctx->arch);
     int nv_major = 0, nv_minor = 0;
     nvrtcVersion(&nv_major, &nv_minor);
@@ -289,6 +283,15 @@ cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_k
         CK(cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
         ctx->libs[key] = lib;
     }
+    *out = lib;
+    return CVG_OK;
+}
+
+cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_key &k,
+                      cudaKernel_t *out, cudaKernel_t *pilot = nullptr)
+{
+    cudaLibrary_t lib = nullptr;
+    CKS(load_module(ctx, make_source(f, k), &lib));
     CK(cudaLibraryGetKernel(out, lib, "cvg_fill_entry"));
     if (pilot) CK(cudaLibraryGetKernel(pilot, lib, "cvg_pilot_entry"));
     return CVG_OK;
@@ -487,6 +490,52 @@ cvg_status check_status(cvg_run_s *r)
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Library-internal helpers used by the batch driver (cvg_internal.h)
+// ---------------------------------------------------------------------------
+cvg_status cvg_internal_fail(cvg_status st, const std::string &msg) { return fail(st, msg); }
+cvg_status cvg_internal_load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *lib)
+{
+    return load_module(ctx, src, lib);
+}
+std::string cvg_internal_fn_struct(const char *name, const cvg_integrand_s &f, int abi,
+                                   int n_params, int grad, const std::string &ns)
+{
+    return fn_struct(name, f, abi, n_params, grad, ns);
+}
+cvg_status cvg_internal_compile_only(const std::string &src, const char *arch, std::string &log)
+{
+    std::vector<char> cubin;
+    return nvrtc_cubin(src, nvrtc_options(arch), cubin, log);
+}
+const char *cvg_internal_src_common() { return cvg_src_common; }
+const char *cvg_internal_src_fill() { return cvg_src_fill; }
+double cvg_internal_now_ms() { return now_ms(); }
+
+void cvg_internal_result(const double *stats, int max_it, int done, int skip, cvg_result *out)
+{
+    // weighted mean over iterations >= skip (src/main.cu:698-714), error
+    // 1/sqrt(sum 1/sigma^2) (src/main.cu:792); chi^2 two-pass
+    const int M = max_it;
+    double sw = 0.0, swr = 0.0;
+    int used = 0;
+    for (int i = skip; i < done; ++i) {
+        sw += 1.0 / stats[M + i];
+        swr += stats[i] / stats[M + i];
+        ++used;
+    }
+    out->result = used ? swr / sw : 0.0;
+    out->error = used ? 1.0 / std::sqrt(sw) : 0.0;
+    double chi2 = 0.0;
+    for (int i = skip; i < done; ++i) {
+        const double dlt = stats[i] - out->result;
+        chi2 += dlt * dlt / stats[M + i];
+    }
+    out->chi2_dof = used > 1 ? chi2 / (used - 1) : 0.0;
+    out->n_it_used = used;
+    out->n_it_done = done;
+}
 
 // ---------------------------------------------------------------------------
 // C ABI
@@ -765,32 +814,14 @@ cvg_status cvg_run_result(cvg_run r, cvg_result *out, double *it_res, double *it
                        r->ctx->stream));
     CKS(check_status(r));
     std::memset(out, 0, sizeof(*out));
-    // weighted mean over iterations >= skip (src/main.cu:698-714), error
-    // 1/sqrt(sum 1/sigma^2) (src/main.cu:792); chi^2 two-pass on the host.
     const int done = std::min(r->it_done, M);
-    double sw = 0.0, swr = 0.0;
-    int used = 0;
-    for (int i = r->p.skip; i < done; ++i) {
-        sw += 1.0 / stats[M + i];
-        swr += stats[i] / stats[M + i];
-        ++used;
-    }
-    out->result = used ? swr / sw : 0.0;
-    out->error = used ? 1.0 / std::sqrt(sw) : 0.0;
-    double chi2 = 0.0;
-    for (int i = r->p.skip; i < done; ++i) {
-        const double dlt = stats[i] - out->result;
-        chi2 += dlt * dlt / stats[M + i];
-    }
-    out->chi2_dof = used > 1 ? chi2 / (used - 1) : 0.0;
+    cvg_internal_result(stats.data(), M, done, r->p.skip, out);
     out->n_strat = r->n_strat;
     out->n_intervals = r->p.n_intervals;
     out->n_cubes = r->n_cubes;
     out->tot_nevals = (int64_t)acc.tot_nevals;
     out->seed = r->p.seed;
     out->gpu_thr = r->p.gpu_thr;
-    out->n_it_used = used;
-    out->n_it_done = done;
     out->precision = r->p.precision;
     if (it_res) for (int i = 0; i < M; ++i) it_res[i] = stats[i];
     if (it_sig2) for (int i = 0; i < M; ++i) it_sig2[i] = stats[M + i];

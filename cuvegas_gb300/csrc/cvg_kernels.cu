@@ -127,10 +127,10 @@ __device__ __forceinline__ dfloat df_add(dfloat a, dfloat b)
     return r;
 }
 
-__global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
+__device__ __forceinline__ void k3_results_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double scratch[3 * 32];
-    const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     double v[3] = {0.0, 0.0, 0.0};   // dh, I, sigma2
     const double vc = a.v_cubes;
     for (int k = 0; k < RIPT; ++k) {
@@ -153,22 +153,25 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
     }
     block_sum<3>(v, scratch);
     if (threadIdx.x == 0) {
-        a.partials[4 * blockIdx.x + 0] = v[0];
-        a.partials[4 * blockIdx.x + 1] = v[1];
-        a.partials[4 * blockIdx.x + 2] = v[2];
-        a.partials[4 * blockIdx.x + 3] = 0.0;
+        a.partials[4 * blk + 0] = v[0];
+        a.partials[4 * blk + 1] = v[1];
+        a.partials[4 * blk + 2] = v[2];
+        a.partials[4 * blk + 3] = 0.0;
     }
 }
+
+__global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a) { k3_results_dev(a, blockIdx.x); }
+
 
 // FP32 form of k3_results.  Per cube, with m = JF/n and q = JF2/n held as
 // double-floats (48-bit significands): I_h / V = m, sigma2_h / V^2 = q - m^2,
 // d_h = (q - m^2)^beta (the constant V^(2 beta) cancels in the allocation).
 // Sums are compensated in FP32 per thread, FP64 across warps and blocks;
 // k3_finish multiplies by V and V^2.
-__global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
+__device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double wsum[4][RB / 32];
-    const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     const float beta = (float)a.beta;
     const int kx = a.scale_exp ? *a.scale_exp : 0;   // work on JF*2^-k, JF2*2^-2k
     dfloat sm = {0.f, 0.f};
@@ -249,14 +252,17 @@ __global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
         for (int w = 0; w < RB / 32; ++w) {
             t0 += wsum[0][w]; t1 += wsum[1][w]; t2 += wsum[2][w]; t3 += wsum[3][w];
         }
-        a.partials[4 * blockIdx.x + 0] = t0;
-        a.partials[4 * blockIdx.x + 1] = t1;
-        a.partials[4 * blockIdx.x + 2] = t2;
-        a.partials[4 * blockIdx.x + 3] = t3;
+        a.partials[4 * blk + 0] = t0;
+        a.partials[4 * blk + 1] = t1;
+        a.partials[4 * blk + 2] = t2;
+        a.partials[4 * blk + 3] = t3;
     }
 }
 
-__global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned nb)
+__global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a) { k3_results_f32_dev(a, blockIdx.x); }
+
+
+__device__ __forceinline__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
 {
     __shared__ double scratch[4 * 32];
     double v[4] = {0.0, 0.0, 0.0, 0.0};
@@ -307,13 +313,16 @@ __global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned n
     }
 }
 
+__global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned nb) { k3_finish_dev(a, nb); }
+
+
 // mode 0: nh from the damped variances (updateNh, src/main.cu:173-187)
 // mode 1: nh_new already holds the counts (initialisation / state import)
 // mode 2: FP32 form, nh = floor(d_h * n_eval_it / sum d_h) in FP32
-__global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
+__device__ __forceinline__ void k3_count_dev(const cvg_realloc_args &a, int mode, const unsigned blk)
 {
     __shared__ cvg_u64 wtot[RB / 32];
-    const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     double dsum = 0.0, n_it = 0.0;
     float scale = 0.f;
     if (mode == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
@@ -354,11 +363,14 @@ __global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
     if (threadIdx.x == 0) {
         cvg_u64 t = 0;
         for (int w = 0; w < RB / 32; ++w) t += wtot[w];
-        a.bsums[blockIdx.x] = t;
+        a.bsums[blk] = t;
     }
 }
 
-__global__ void __launch_bounds__(1024) k3_scan(cvg_realloc_args a, unsigned nb)
+__global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode) { k3_count_dev(a, mode, blockIdx.x); }
+
+
+__device__ __forceinline__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb)
 {
     __shared__ cvg_u64 scratch[33];
     const unsigned per = (nb + blockDim.x - 1) / blockDim.x;
@@ -373,12 +385,15 @@ __global__ void __launch_bounds__(1024) k3_scan(cvg_realloc_args a, unsigned nb)
     if (threadIdx.x == 0) a.bsums[nb] = total;
 }
 
-__global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb)
+__global__ void __launch_bounds__(1024) k3_scan(cvg_realloc_args a, unsigned nb) { k3_scan_dev(a, nb); }
+
+
+__device__ __forceinline__ void k3_apply_dev(const cvg_realloc_args &a, unsigned nb, const unsigned blk)
 {
     __shared__ cvg_u32 sh[CVG_REALLOC_CHUNK];
     __shared__ cvg_u64 st[CVG_REALLOC_CHUNK];
     __shared__ cvg_u64 scratch[33];
-    const cvg_u32 base = blockIdx.x * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     const cvg_u32 cnt = min((cvg_u32)CVG_REALLOC_CHUNK, a.n_cubes - base);
     for (int i = threadIdx.x; i < CVG_REALLOC_CHUNK; i += RB)
         sh[i] = (cvg_u32)i < cnt ? a.nh_new[base + i] : 0u;
@@ -388,7 +403,7 @@ __global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb)
     for (int k = 0; k < RIPT; ++k) local += sh[threadIdx.x * RIPT + k];
     cvg_u64 off = local;
     block_exscan_u64(off, scratch);
-    off += a.bsums[blockIdx.x];
+    off += a.bsums[blk];
     const cvg_u64 TS = (cvg_u64)a.tile_samples;
 #pragma unroll 1
     for (int k = 0; k < RIPT; ++k) {
@@ -404,8 +419,11 @@ __global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb)
     }
     __syncthreads();
     for (int i = threadIdx.x; i < (int)cnt; i += RB) a.nh_sum[base + i] = st[i];
-    if (blockIdx.x == nb - 1 && threadIdx.x == 0) a.nh_sum[a.n_cubes] = a.bsums[nb];
+    if (blk == nb - 1 && threadIdx.x == 0) a.nh_sum[a.n_cubes] = a.bsums[nb];
 }
+
+__global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb) { k3_apply_dev(a, nb, blockIdx.x); }
+
 
 // ---------------------------------------------------------------------------
 // K4: grid refinement, FP64.  One thread-block cluster of CL CTAs per
@@ -423,14 +441,13 @@ __device__ __forceinline__ double cl_sum(cg::cluster_group &cl, double *slot)
     return t;
 }
 
-__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine(cvg_refine_args a)
+__device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const int d)
 {
     extern __shared__ __align__(16) double ks[];
     __shared__ double part[4];
     __shared__ double wscr[KB / 32];
     cg::cluster_group cl = cg::this_cluster();
     const int r = (int)cl.block_rank();
-    const int d = blockIdx.x / CL;
     const int N = a.n_intervals, tid = threadIdx.x;
     const int B = (N + CL - 1) / CL;
     const int i0 = min(N, r * B), i1 = min(N, i0 + B), nb = i1 - i0;
@@ -551,6 +568,100 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine(cvg_r
     cl.sync();   // keep shared memory alive until every CTA has read it
 }
 
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine(cvg_refine_args a)
+{
+    k4_refine_dev(a, blockIdx.x / CL);
+}
+
+// ---------------------------------------------------------------------------
+// Batched forms: one launch covers the blocks (or clusters) of every
+// instance; a block finds its instance by binary search over the prefix of
+// blocks per instance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_inst(const unsigned *base, int n, unsigned b)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(RB) k3_results_b(cvg_realloc_batch B)
+{
+    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const cvg_realloc_args a = B.A[i];
+    if (a.fast_pow) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
+    else k3_results_dev(a, blockIdx.x - B.blk_base[i]);
+}
+
+__global__ void __launch_bounds__(1024) k3_finish_b(cvg_realloc_batch B)
+{
+    const cvg_realloc_args a = B.A[blockIdx.x];
+    k3_finish_dev(a, cvg_realloc_blocks(a.n_cubes));
+}
+
+__global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
+{
+    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const cvg_realloc_args a = B.A[i];
+    if (!a.adapt && mode != 1) return;
+    k3_count_dev(a, mode == 0 ? (a.fast_pow ? 2 : 0) : mode, blockIdx.x - B.blk_base[i]);
+}
+
+__global__ void __launch_bounds__(1024) k3_scan_b(cvg_realloc_batch B, int mode)
+{
+    const cvg_realloc_args a = B.A[blockIdx.x];
+    if (!a.adapt && mode != 1) return;
+    k3_scan_dev(a, cvg_realloc_blocks(a.n_cubes));
+}
+
+__global__ void __launch_bounds__(RB) k3_apply_b(cvg_realloc_batch B, int mode)
+{
+    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const cvg_realloc_args a = B.A[i];
+    if (!a.adapt && mode != 1) return;
+    k3_apply_dev(a, cvg_realloc_blocks(a.n_cubes), blockIdx.x - B.blk_base[i]);
+}
+
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine_b(cvg_refine_batch B)
+{
+    const unsigned cid = blockIdx.x / CL;
+    const int i = find_inst(B.dim_base, B.n, cid);
+    k4_refine_dev(B.R[i], (int)(cid - B.dim_base[i]));
+}
+
+// Global tile numbering of the next batched fill: tile_base[i] = first tile
+// of instance i, tile_base[n] = total (tiles per instance clamped to the
+// capacity of its tile map).
+__global__ void k_tile_base(cvg_realloc_batch B, cvg_u64 *tile_base)
+{
+    __shared__ cvg_u64 cnt[1024];
+    cvg_u64 carry = 0;
+    for (int b0 = 0; b0 < B.n; b0 += blockDim.x) {
+        const int i = b0 + threadIdx.x;
+        cvg_u64 c = 0;
+        if (i < B.n) {
+            const cvg_realloc_args &a = B.A[i];
+            const cvg_u64 S = a.nh_sum[a.n_cubes], TS = (cvg_u64)a.tile_samples;
+            c = (S + TS - 1) / TS;
+            if (c > a.max_tiles) c = a.max_tiles;
+        }
+        cnt[threadIdx.x] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < (int)blockDim.x && b0 + k < B.n; ++k) {
+                const cvg_u64 v = cnt[k];
+                tile_base[b0 + k] = carry;
+                carry += v;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tile_base[B.n] = carry;
+}
+
 __global__ void grid32(const double *x, float *x32, int n)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -658,5 +769,43 @@ cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s
     cvg_u64 blocks = (n + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     fill_u32<<<(unsigned)blocks, 256, 0, s>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
+                                     cvg_u64 *tile_base, cudaStream_t s)
+{
+    (void)fast;
+    k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);
+    k3_finish_b<<<B.n, 1024, 0, s>>>(B);
+    if (adapt) {
+        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
+        k3_scan_b<<<B.n, 1024, 0, s>>>(B, 0);
+        k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
+    }
+    k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_base, cudaStream_t s)
+{
+    k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
+    k3_scan_b<<<B.n, 1024, 0, s>>>(B, 1);
+    k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
+    k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_refine_batch(const cvg_refine_batch &B, int n_intervals, cudaStream_t s)
+{
+    const int N = n_intervals, Bk = (N + CL - 1) / CL;
+    const size_t smem = sizeof(double) * ((size_t)(Bk + 2) + 2 * Bk + 2 * (size_t)N + N + 1) +
+                        sizeof(int) * (size_t)N + 16;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k4_refine_b, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k4_refine_b<<<B.total_dims * CL, KB, smem, s>>>(B);
     return cudaGetLastError();
 }

@@ -61,7 +61,21 @@ struct cvg_refine_args {
 
 enum { CVG_REALLOC_CHUNK = 2048, CVG_REFINE_BLOCK = 1024, CVG_REFINE_MAX_N = 4096 };
 
-inline unsigned cvg_realloc_blocks(cvg_u32 n_cubes)
+// Device tables of a batch of instances (one launch covers all of them).
+struct cvg_realloc_batch {
+    const cvg_realloc_args *A;    // [n]
+    const unsigned *blk_base;     // [n+1] prefix of reallocation blocks
+    unsigned total_blocks;
+    int n;
+};
+struct cvg_refine_batch {
+    const cvg_refine_args *R;     // [n]
+    const unsigned *dim_base;     // [n+1] prefix of dimensions
+    unsigned total_dims;
+    int n;
+};
+
+__host__ __device__ inline unsigned cvg_realloc_blocks(cvg_u32 n_cubes)
 {
     return (unsigned)((n_cubes + CVG_REALLOC_CHUNK - 1) / CVG_REALLOC_CHUNK);
 }
@@ -79,6 +93,12 @@ cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, 
 cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cudaStream_t s);
 // Fill n words with a value.
 cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
+
+// Batched reallocation (+ the tile numbering of the next batched fill).
+cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
+                                     cvg_u64 *tile_base, cudaStream_t s);
+cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_base, cudaStream_t s);
+cudaError_t cvg_launch_refine_batch(const cvg_refine_batch &B, int n_intervals, cudaStream_t s);
 
 // Set the calling thread's cvg_last_error() message (host code of the library).
 void cvg_internal_set_error(const char *msg);

@@ -72,6 +72,7 @@ class Integrand:
 
     def __init__(self, ctx, source, n_dim, n_params=0, has_grad=False, abi=L.ABI_NATIVE):
         self.ctx = ctx
+        self.source = source
         self.n_dim = int(n_dim)
         self.n_params = int(n_params)
         self.has_grad = bool(has_grad)

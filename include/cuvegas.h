@@ -186,6 +186,47 @@ cvg_status cvg_run_last_fill_ms(cvg_run r, float *ms);
  * (CVG_FLAG_TIME_FILL); synchronises.  At most `cap` values; *n = count. */
 cvg_status cvg_run_fill_times(cvg_run r, float *ms, int32_t cap, int32_t *n);
 
+/* ---- batched integration ---- */
+
+typedef struct cvg_batch_s *cvg_batch;
+
+/* One integral of a batch. */
+typedef struct {
+    int32_t n_dim;        /* 1..16                                                  */
+    int32_t n_strat;      /* 0 = (int)pow(evals per iteration / 4, 1/n_dim)         */
+    int64_t tot_eval;     /* evaluations over all iterations (common max_it)        */
+    uint32_t instance;    /* Philox stream id: equal to a single run with the same id */
+    int32_t pad;
+} cvg_instance;
+
+/* Many independent integrals of one integrand family (one source; parameters
+ * per instance) with different dimensions and evaluation counts, advanced
+ * together: per iteration one persistent fill launch for the whole batch,
+ * batched grid refinement and batched reallocation; with CVG_FLAG_GRAPH the
+ * iteration is one CUDA-graph launch.  No counterpart in the reference (it
+ * integrates one function per call, cuda_wrapper.cu:290).
+ * params_per_dim[d] (d = 0..16) = parameters of the dimension-d integrand;
+ * theta = the instances' parameters back to back.  `common` supplies max_it,
+ * skip, n_intervals, alpha, beta, seed, precision, flags, block, spt. */
+cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, int32_t n,
+                            const cvg_instance *inst, const int32_t *params_per_dim,
+                            const double *theta, const cvg_params *common, cvg_batch *out);
+cvg_status cvg_batch_destroy(cvg_batch b);
+/* Enqueue n iterations of every instance (no host synchronisation). */
+cvg_status cvg_batch_iterate(cvg_batch b, int32_t n);
+/* Synchronise; out[n], it_res / it_sig2 [n][max_it] (may be NULL). */
+cvg_status cvg_batch_results(cvg_batch b, cvg_result *out, double *it_res, double *it_sig2);
+/* Launch shape and the samples of the next batched fill (synchronises). */
+cvg_status cvg_batch_info_get(cvg_batch b, int32_t *block, int32_t *spt, int32_t *grid,
+                              int64_t *fill_smem_bytes, int64_t *next_samples);
+/* Device time of the last timed batched fill (eager iterations). */
+cvg_status cvg_batch_last_fill_ms(cvg_batch b, float *ms);
+/* NVRTC-only compile of the batched kernels for the given dimensions (no GPU
+ * needed), for build checks; `log` (may be NULL) receives the NVRTC log. */
+cvg_status cvg_batch_compile_check(const char *source, int32_t n_dims, const int32_t *dims,
+                                   const int32_t *params_per_dim, int32_t precision,
+                                   int32_t block, const char *arch, char *log, size_t log_len);
+
 /* ---- reallocation without allocation ----
  * For callers that cannot call cudaMalloc (code running inside another
  * framework's memory pool, or with all device memory reserved up front).

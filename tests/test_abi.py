@@ -70,3 +70,8 @@ def test_bad_arguments_rejected():
     assert e.value.status == L.ERR_INVALID
     with pytest.raises(L.CuvegasError):
         L.compile_check(I.GAUSS, 33)
+
+
+def test_batch_kernels_compile():
+    L.batch_compile_check(I.PRODPEAK, list(range(2, 13)), [2 * d for d in range(17)],
+                          precision=L.PREC_FP32)
