@@ -332,11 +332,12 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.quick and not args.no_cpu:
-        n_cpu = 2_000_000
+        n_cpu = N_IT          # the workload's own size per iteration, 3 iterations
         rate, tot, dt = cpu_oracle_rate(n_cpu, 3)
         cpu = {"value": rate, "unit": "evals/s", "cores": os.cpu_count(), "kind": "port",
                "sample": "3 VEGAS+ iterations of the same d=8 Gaussian workload at %d "
-                         "evals/iteration, FP64 CPU oracle, %d evals in %.1f s" % (n_cpu, tot, dt)}
+                         "evals/iteration, FP64 CPU oracle on all host cores, %d evals in %.1f s"
+                         % (n_cpu, tot, dt)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
@@ -357,6 +358,166 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_workload(args):
+    """Lines for the other benchmark configurations (one JSON line each)."""
+    import numpy as np
+    import torch
+    from cuvegas_gb300 import _build, _lib as L, runtime, integrands as I
+    from oracle import analytic as A
+    _build.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream(device=0)
+    ctx = runtime.Context(0, stream=C_stream(stream))
+    out = {"workload": args.workload, "n_gpus": 1, "data": "synthetic"}
+
+    def run_timed(f, dim, n_it, iters, prec, theta=None, skip=5):
+        # iterations timed as CUDA-graph replays; fill launch times from an
+        # eager run of the same workload (events around each fill)
+        p = runtime.make_params(dim, n_it * iters, iters, skip=skip, n_intervals=1024, seed=0,
+                                precision=prec, flags=L.FLAG_TIME_FILL)
+        with runtime.Run(f, p, theta) as r:
+            r.iterate(iters)
+            fills = r.fill_times()[1:]
+        p = runtime.make_params(dim, n_it * iters, iters, skip=skip, n_intervals=1024, seed=0,
+                                precision=prec, flags=L.FLAG_GRAPH)
+        with runtime.Run(f, p, theta) as r:
+            r.iterate(1)          # warm (graph capture, first adaptation): not timed
+            r.sync()
+            with ClockSampler(0) as clk:
+                it_ms = timed_iterations(r, iters - 1, stream, torch)
+            res, it_res, it_sig = r.result()
+            st = r.get(L.BUF_STATS)
+            info = r.info
+        ev = float(st[2, 1:iters].sum())
+        return dict(res=res, it_res=it_res, it_sig=it_sig, it_ms=it_ms, fills=fills, evals=ev,
+                    ms=float(sum(it_ms)), clk=clk.summary(), info=info, samples=st[2])
+
+    if args.workload in ("c1", "c5"):
+        if args.workload == "c1":
+            dim, n_it, iters, src, th, P = 4, args.evals or 1_000_000, 10, I.GAUSS, None, 0
+            exact = A.gauss_normalised(4)
+            forms = [("plain", L.PREC_FP64), ("chosen", L.PREC_FP32)]
+        else:
+            dim, n_it, iters, src = 16, args.evals or 1_000_000_000, 20, I.CORNER
+            th, P = I.corner_theta(0, 16), 16
+            exact = A.corner_peak(th)
+            forms = [("chosen", L.PREC_FP32), ("plain", L.PREC_FP64)]
+        f = ctx.integrand(src, dim, n_params=P)
+        for name, prec in forms:
+            if name == "plain" and args.workload == "c5" and args.quick:
+                continue
+            m = run_timed(f, dim, n_it, iters, prec, th)
+            t, nit, _, _ = time_to_rel(m["it_res"], m["it_sig"], [0.0] + m["it_ms"], 5,
+                                       exact=exact)
+            fill_ms = float(np.mean(m["fills"]))
+            step_ms = m["ms"] / (iters - 1)
+            d = {"value": m["evals"] / (m["ms"] / 1e3), "unit": "evals/s", "ms_per_step": step_ms,
+                 "fill_ms_mean": fill_ms, "realloc_refine_ms": step_ms - fill_ms,
+                 "result": m["res"].result, "error": m["res"].error, "exact": exact,
+                 "pull": (m["res"].result - exact) / m["res"].error, "chi2_dof": m["res"].chi2_dof,
+                 "time_to_1e-4_s": t, "clocks": m["clk"], "n_cubes": m["info"].n_cubes,
+                 "dtype": "f32" if prec == L.PREC_FP32 else "f64"}
+            # reallocation traffic: ~72 algorithmic bytes per hypercube and iteration
+            d["realloc_algorithmic_gbs"] = 72.0 * m["info"].n_cubes / ((step_ms - fill_ms) * 1e-3) / 1e9
+            out[name] = d
+        if args.workload == "c1" and not args.no_cpu:
+            rate_t = time.perf_counter()
+            from oracle import pyoracle as Po
+            u, _ = Po.uniforms(Po.U_PHILOX_F64, seed=0)
+            o = Po.integrate(Po.F_GAUSS, 4, n_it * iters, iters, theta=np.array([0.5, 0.1]),
+                             skip=5, u=u)
+            dt = time.perf_counter() - rate_t
+            out["cpu_baseline"] = {"value": o["tot_nevals"] / dt, "unit": "evals/s",
+                                   "cores": os.cpu_count(), "kind": "port",
+                                   "sample": "the whole C1 run (10 x 1e6), FP64 oracle",
+                                   "result": o["result"], "error": o["error"]}
+        if "plain" in out:
+            out["speedup_chosen_vs_plain"] = out["chosen"]["value"] / out["plain"]["value"]
+    elif args.workload == "c3":
+        from cuvegas_gb300 import autograd as AG
+        th = I.mixture_theta(0, 6)
+        f = ctx.integrand(I.MIXTURE, 6, n_params=16, has_grad=True)
+        for name, prec in (("chosen", L.PREC_FP32), ("plain", L.PREC_FP64)):
+            p = runtime.make_params(6, 10_000_000 * 15, 15, skip=5, n_intervals=1024, seed=0,
+                                    precision=prec)
+            AG.forward_with_grad(f, runtime.make_params(6, 4 * 200000, 4, skip=1,
+                                                        n_intervals=1024, precision=prec), th)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Ival, err, G, g_it, _, res = AG.forward_with_grad(f, p, th)
+            dt = time.perf_counter() - t0
+            gex = A.mixture_grad(th, 6)
+            sg = g_it.std(axis=0, ddof=1) / np.sqrt(len(g_it))
+            out[name] = {"forward_backward_s": dt, "result": Ival, "error": err,
+                         "exact": A.mixture(th, 6), "chi2_dof": res.chi2_dof,
+                         "grad_max_err_vs_analytic_rel_to_max": float(
+                             np.max(np.abs(G - gex)) / np.max(np.abs(gex))),
+                         "grad_max_pull_vs_analytic": float(np.max(np.abs(G - gex) / sg)),
+                         "evals": int(res.tot_nevals)}
+        # same-seed finite differences of the frozen-state estimator, FP32
+        p = runtime.make_params(6, 1_000_000 * 6, 6, skip=3, n_intervals=1024, seed=1,
+                                precision=L.PREC_FP32)
+        _, _, G, _, recs, _ = AG.forward_with_grad(f, p, th, record=True)
+        h, worst = 1e-4, 0.0
+        for k in range(16):
+            tp, tm = th.copy(), th.copy()
+            tp[k] += h
+            tm[k] -= h
+            fd = (AG.replay_estimates(f, p, tp, recs)[0] - AG.replay_estimates(f, p, tm, recs)[0]) / (2 * h)
+            worst = max(worst, abs(G[k] - fd) / max(abs(fd), 1e-12))
+        out["grad_max_rel_err_vs_fd_h1e-4"] = worst
+    elif args.workload == "c4":
+        from cuvegas_gb300 import autotune, batch as B
+        insts = I.batch_instances(0, 512)
+        ppd = [2 * d for d in range(17)]
+        block, spt = autotune.tune_batch(ctx, I.PRODPEAK, insts, ppd, L.PREC_FP32)
+        with B.Batch(ctx, I.PRODPEAK, insts, ppd, max_it=10, skip=5, seed=0,
+                     precision=L.PREC_FP32, graph=True, block=block, spt=spt) as b:
+            b.iterate(1)
+            torch.cuda.synchronize()
+            evs = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            with ClockSampler(0) as clk:
+                evs[0].record(stream)
+                b.iterate(9)
+                evs[1].record(stream)
+                stream.synchronize()
+            ms = evs[0].elapsed_time(evs[1])
+            res, it_res, it_sig = b.results()
+        ev = sum(r.tot_nevals for r in res)
+        ev_timed = ev * 0.9          # iterations 2..10 (all instances have ~constant counts)
+        pulls = []
+        for r, inst in zip(res, insts):
+            ex = A.product_peak(inst["c"], inst["u"])
+            pulls.append((r.result - ex) / r.error)
+        pulls = np.abs(np.array(pulls))
+        out["chosen"] = {"value": ev_timed / (ms / 1e3), "unit": "evals/s", "ms_per_step": ms / 9,
+                         "block": block, "spt": spt, "graph": True, "instances": len(insts),
+                         "evals_per_iteration": ev / 10, "clocks": clk.summary(),
+                         "frac_within_4sigma": float(np.mean(pulls < 4)),
+                         "max_pull": float(pulls.max())}
+        # plain form: FP64, one integral per call (the reference's interface shape)
+        for d in range(2, 13):    # compile every dimension first (JIT is not timed)
+            fi = ctx.integrand(I.PRODPEAK, d, n_params=2 * d)
+            runtime.integrate_once(fi, runtime.make_params(d, 4 * 4000, 4, skip=1,
+                                                           precision=L.PREC_FP64),
+                                   np.ones(2 * d))
+        t0 = time.perf_counter()
+        ev_p = 0
+        n_plain = 64
+        for i, inst in enumerate(insts[:n_plain]):
+            d = inst["dim"]
+            fi = ctx.integrand(I.PRODPEAK, d, n_params=2 * d)
+            p = runtime.make_params(d, inst["n_eval_it"] * 10, 10, skip=5, n_intervals=1024,
+                                    seed=0, precision=L.PREC_FP64, instance=i)
+            r, _, _ = runtime.integrate_once(fi, p, inst["theta"])
+            ev_p += r.tot_nevals
+        dt = time.perf_counter() - t0
+        out["plain"] = {"value": ev_p / dt, "unit": "evals/s", "instances_timed": n_plain,
+                        "note": "FP64, cvg_integrate per instance (JIT cached after first use)"}
+        out["speedup_chosen_vs_plain"] = out["chosen"]["value"] / out["plain"]["value"]
+    print(json.dumps(out), flush=True)
+
+
 def C_stream(stream):
     import ctypes
     return ctypes.c_void_p(stream.cuda_stream)
@@ -370,6 +531,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="headline number only")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2 is the headline line; the others print their own line")
     ap.add_argument("--evals", type=int, default=0,
                     help="evals/iteration override (profiling runs on a smaller case)")
     args = ap.parse_args()
@@ -380,6 +543,8 @@ def main():
         N_IT = args.evals
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "c2":
+        run_workload(args)
     else:
         run_ours(args)
 

@@ -53,6 +53,7 @@ struct inst_host {
     float *x_edges32;
     cvg_u32 *counts, *nh_new, *tile_cube, *iteration;
     int *scale_exp;
+    cvg_u32 *done;
     cvg_u64 *nh_sum, *bsums;
     cvg_acc_dev *acc;
 };
@@ -80,7 +81,7 @@ struct cvg_batch_s {
     size_t fill_smem = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -113,10 +114,10 @@ std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
     char entry[512];
     std::snprintf(entry, sizeof(entry),
                   "extern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_batch_entry("
-                  "const cvg_batch_args b) { cvg_fill_batch<%s, %d, cvg_disp>(b); }\n"
+                  "const cvg_batch_args b) { cvg_fill_batch<%s, %d, cvg_disp, %d>(b); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_batch_entry("
                   "const cvg_batch_args b) { cvg_pilot_batch<%s, 8, cvg_disp>(b); }\n",
-                  b.block, T, b.block, T);
+                  b.block, T, b.block, b.p.n_intervals, T);
     s += entry;
     return s;
 }
@@ -159,9 +160,15 @@ cvg_status enqueue_iteration(cvg_batch_s *b, bool timed)
     if (timed) BCK(cudaEventRecord(b->ev0, s));
     BCK(cudaLaunchKernel((const void *)b->fill, dim3(b->grid), dim3(b->block), args, b->fill_smem, s));
     if (timed) BCK(cudaEventRecord(b->ev1, s));
-    BCK(cvg_launch_refine_batch(refine_batch(b), b->p.n_intervals, s));
+    // refinement on the second stream, beside the reallocation
+    cudaStream_t aux = b->ctx->aux;
+    BCK(cudaEventRecord(b->ev_fork, s));
+    BCK(cudaStreamWaitEvent(aux, b->ev_fork, 0));
+    BCK(cvg_launch_refine_batch(refine_batch(b), b->p.n_intervals, aux));
+    BCK(cudaEventRecord(b->ev_join, aux));
     BCK(cvg_launch_realloc_batch(realloc_batch(b), (b->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1,
                                  b->p.precision == CVG_PREC_FP32, b->d_tile_base, s));
+    BCK(cudaStreamWaitEvent(s, b->ev_join, 0));
     return CVG_OK;
 }
 
@@ -288,7 +295,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         h.acc = (cvg_acc_dev *)take(sizeof(cvg_acc_dev));
         h.iteration = (cvg_u32 *)take(16);
         h.scale_exp = (int *)take(16);
-        take(16);
+        h.done = (cvg_u32 *)take(16);
         h.theta = (double *)take(sizeof(double) * std::max(1, h.n_params));
         h.grad = (double *)take(sizeof(double) * std::max(1, h.n_params));
         // uniform grid (src/main.cu:432-441)
@@ -341,6 +348,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         r.iteration = h.iteration;
         r.status = b->d_status;
         r.scale_exp = a.scale_exp;
+        r.done = h.done;
         r.max_tiles = h.max_tiles;
         r.n_eval_it = h.n_eval_it;
         r.v_cubes = h.v_cubes;
@@ -394,6 +402,8 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     b->grid = occ * ctx->n_sm;
     BCK(cudaEventCreate(&b->ev0));
     BCK(cudaEventCreate(&b->ev1));
+    BCK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    BCK(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
     // FP32 form: per-instance scale exponent from a pilot evaluation
     if (p.precision == CVG_PREC_FP32) {
         std::vector<int> ex(n, -1000);
@@ -423,6 +433,8 @@ cvg_status cvg_batch_destroy(cvg_batch b)
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     if (b->arena) cudaFree(b->arena);
     delete b;
     return CVG_OK;

@@ -90,13 +90,12 @@ CVG_D cvg_u32x4 cvg_philox(cvg_u32 c0, cvg_u32 c1, cvg_u32 c2, cvg_u32 c3, cvg_u
 #pragma unroll
     for (int r = 0; r < 10; ++r) {
         if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-        const cvg_u32 lo0 = 0xD2511F53u * c0;
-        const cvg_u32 hi0 = __umulhi(0xD2511F53u, c0);
-        const cvg_u32 lo1 = 0xCD9E8D57u * c2;
-        const cvg_u32 hi1 = __umulhi(0xCD9E8D57u, c2);
-        const cvg_u32 n0 = hi1 ^ c1 ^ k0;
-        const cvg_u32 n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        // one 32x32->64 multiply per word pair (high and low halves together)
+        const cvg_u64 p0 = (cvg_u64)0xD2511F53u * c0;
+        const cvg_u64 p1 = (cvg_u64)0xCD9E8D57u * c2;
+        const cvg_u32 n0 = (cvg_u32)(p1 >> 32) ^ c1 ^ k0;
+        const cvg_u32 n2 = (cvg_u32)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (cvg_u32)p1; c2 = n2; c3 = (cvg_u32)p0;
     }
     cvg_u32x4 o; o.x = c0; o.y = c1; o.z = c2; o.w = c3;
     return o;

@@ -213,7 +213,8 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
 
 // One tile: samples [tile*TS, min((tile+1)*TS, S)).  Returns false (and sets a
 // status bit) if the tile map is inconsistent; uniform across the block.
-template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F>
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
+          int NI>
 CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                          const cvg_fill_ctx<T> &cx, cvg_u64 tile, cvg_u64 n_tiles, cvg_u64 S,
                          cvg_acc<T> *gacc)
@@ -222,7 +223,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
     constexpr int NB = (D + 3) / 4;
     constexpr bool H = HSM && !GRAD;
     const int tid = threadIdx.x;
-    const int TS = a.tile_samples, N = cx.N, ns = cx.ns;
+    const int TS = a.tile_samples, N = NI > 0 ? NI : cx.N, ns = cx.ns;   // NI: bins fixed at compile time
     const T dy = cx.dy, fN = cx.fN, fNm1 = cx.fNm1;
     const T *G = cx.G;
     int *starts = sm.starts;
@@ -292,33 +293,31 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 j = 0u;
             }
             ++run;
-            cvg_u32 rr[NB * 4];
-            if (!REPLAY) {
-#pragma unroll
-                for (int b = 0; b < NB; ++b) {
-                    const cvg_u32x4 r4 = cvg_philox(j, c, cx.it, (cvg_u32)b | cx.c3, cx.k0, cx.k1);
-                    rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y;
-                    rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
-                }
-            }
             T x[D];
             int bin[D];
             T jac = cx.jac0;
 #pragma unroll
-            for (int d = 0; d < D; ++d) {
-                T u;
-                if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
-                else u = cvg_uniform<T>(rr[d]);
-                const T y = cvg_fma(u, dy, cdy[d]);
-                const T z = y * fN;
-                T frac;
-                const int b = cvg_bin(z, N, fNm1, frac);
-                const T e0 = G[d * (N + 1) + b];
-                const T e1 = G[d * (N + 1) + b + 1];
-                const T dx = e1 - e0;
-                x[d] = cvg_fma(dx, frac, e0);
-                jac *= fN * dx;
-                bin[d] = b;
+            for (int bk = 0; bk < NB; ++bk) {   // 4 dimensions per Philox call
+                cvg_u32x4 r4;
+                if (!REPLAY) r4 = cvg_philox(j, c, cx.it, (cvg_u32)bk | cx.c3, cx.k0, cx.k1);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int d = 4 * bk + q;
+                    if (d >= D) break;
+                    T u;
+                    if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
+                    else u = cvg_uniform<T>(q == 0 ? r4.x : q == 1 ? r4.y : q == 2 ? r4.z : r4.w);
+                    const T y = cvg_fma(u, dy, cdy[d]);
+                    const T z = y * fN;
+                    T frac;
+                    const int b = cvg_bin(z, N, fNm1, frac);
+                    const T e0 = G[d * (N + 1) + b];
+                    const T e1 = G[d * (N + 1) + b + 1];
+                    const T dx = e1 - e0;
+                    x[d] = cvg_fma(dx, frac, e0);
+                    jac *= fN * dx;
+                    bin[d] = b;
+                }
             }
             if (GRAD) {
                 T g[PP];
@@ -361,12 +360,12 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 }
 
 // Add the CTA's shared-memory bin histograms to the global FP64/u32 ones.
-template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD>
+template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD, int NI>
 CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm)
 {
     if (!(HSM && !GRAD)) return;
     __syncthreads();
-    const int N = a.n_intervals;
+    const int N = NI > 0 ? NI : a.n_intervals;
     for (int i = threadIdx.x; i < D * N; i += BS) {
         const cvg_u32 cn = sm.hc[i];
         if (cn) {
@@ -379,7 +378,8 @@ CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
 
 // Persistent single-instance fill: this CTA takes tiles blockIdx.x,
 // blockIdx.x + gridDim.x, ...
-template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F>
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
+          int NI = 0>
 CVG_D void cvg_fill_body(const cvg_fill_args &a)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
@@ -404,10 +404,11 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     __syncthreads();
 
     for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
-        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F>(a, sm, cx, tile, n_tiles, S, gacc))
+        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI>(a, sm, cx, tile, n_tiles, S,
+                                                                      gacc))
             break;
 
-    cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD>(a, sm);
+    cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI>(a, sm);
     if (GRAD) {
         const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
@@ -438,7 +439,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 template <int V> struct cvg_int { static constexpr int value = V; };
 
 
-template <typename T, int BS, class DISP>
+template <typename T, int BS, class DISP, int NI = 0>
 CVG_D void cvg_fill_batch(const cvg_batch_args &b)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
@@ -469,10 +470,10 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
             const cvg_u64 S = a.nh_sum[a.n_cubes];
             const cvg_u64 nt = b.tile_base[i + 1] - tb;
             for (cvg_u64 lt = t - tb; lt < te - tb; ++lt)
-                if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F>(a, sm, cx, lt, nt, S,
-                                                                             nullptr))
+                if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI>(a, sm, cx, lt, nt,
+                                                                                 S, nullptr))
                     break;
-            cvg_fill_flush<D, T, BS, true, true, P, false>(a, sm);
+            cvg_fill_flush<D, T, BS, true, true, P, false, NI>(a, sm);
         });
         t = te;
     }

@@ -105,6 +105,7 @@ struct cvg_run_s {
     cvg_u32 *counts = nullptr, *nh_new = nullptr, *tile_cube = nullptr, *iteration = nullptr;
     cvg_u32 *status = nullptr;
     int *scale_exp = nullptr;
+    cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
     size_t ubuf_samples = 0;
@@ -116,6 +117,7 @@ struct cvg_run_s {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fill_ev;   // timed fills
     size_t fill_ev_used = 0;
     cudaEvent_t ev0_own = nullptr, ev1_own = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;   // refinement beside reallocation
 };
 
 // ---------------------------------------------------------------------------
@@ -165,7 +167,7 @@ void write_file(const std::string &p, const std::vector<char> &data)
 }
 
 struct variant_key {
-    int dim, prec, block, esm, hsm, replay, n_params, grad, abi;
+    int dim, prec, block, esm, hsm, replay, n_params, grad, abi, nbins;
 };
 
 // Integrand adaptor type F of the fill templates: static f (value) and df
@@ -206,12 +208,12 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     char entry[1024];
     std::snprintf(entry, sizeof(entry),
                   "\nextern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_entry("
-                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s, cvg_fn_user>(a); }\n"
+                  "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s, cvg_fn_user, %d>(a); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_entry("
                   "const cvg_fill_args a) { cvg_pilot_body<%d, %s, 256, %d, cvg_fn_user>(a, blockIdx.x); }\n",
                   k.block, k.dim, T, k.block, k.esm ? "true" : "false",
                   k.hsm ? "true" : "false", k.replay ? "true" : "false", k.n_params,
-                  k.grad ? "true" : "false", k.dim, T, k.n_params);
+                  k.grad ? "true" : "false", k.nbins, k.dim, T, k.n_params);
     s += entry;
     return s;
 }
@@ -302,7 +304,7 @@ cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v
     cvg_context ctx = r->ctx;
     const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
     variant_key k{r->f->dim, r->p.precision, r->block, r->esm, r->hsm, replay ? 1 : 0,
-                  r->f->n_params, grad ? 1 : 0, r->f->abi};
+                  r->f->n_params, grad ? 1 : 0, r->f->abi, r->p.n_intervals};
     if (grad) k.hsm = 0;
     const cvg_u64 smem = cvg_fill_smem_bytes(k.dim, r->p.n_intervals, tsz, k.esm, k.hsm, k.grad,
                                              r->TS, k.n_params, k.block);
@@ -351,6 +353,7 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.iteration = r->iteration;
     a.status = r->status;
     a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
+    a.done = r->done;
     a.max_tiles = r->max_tiles;
     a.n_eval_it = r->n_eval_it;
     a.v_cubes = r->v_cubes;
@@ -474,8 +477,20 @@ cvg_status enqueue_stages(cvg_run_s *r, int stages, bool timed)
             CKS(launch_fill(r, r->fill, timed));
         }
     }
-    if (stages & CVG_STAGE_REFINE) CK(cvg_launch_refine(refine_args(r), s));
-    if (stages & CVG_STAGE_REALLOC) CK(cvg_launch_realloc(realloc_args(r), s));
+    if ((stages & CVG_STAGE_REFINE) && (stages & CVG_STAGE_REALLOC)) {
+        // independent: the grid refinement (few CTAs, latency bound) overlaps the
+        // reallocation (HBM bound); joined before the next fill
+        cudaStream_t aux = r->ctx->aux;
+        CK(cudaEventRecord(r->ev_fork, s));
+        CK(cudaStreamWaitEvent(aux, r->ev_fork, 0));
+        CK(cvg_launch_refine(refine_args(r), aux));
+        CK(cudaEventRecord(r->ev_join, aux));
+        CK(cvg_launch_realloc(realloc_args(r), s));
+        CK(cudaStreamWaitEvent(s, r->ev_join, 0));
+    } else {
+        if (stages & CVG_STAGE_REFINE) CK(cvg_launch_refine(refine_args(r), s));
+        if (stages & CVG_STAGE_REALLOC) CK(cvg_launch_realloc(realloc_args(r), s));
+    }
     return CVG_OK;
 }
 
@@ -565,6 +580,8 @@ cvg_status cvg_context_create(int device, void *stream, cvg_context *out)
     char arch[32];
     std::snprintf(arch, sizeof(arch), "sm_%d%da", prop.major, prop.minor);
     c->arch = arch;
+    e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return fail(CVG_ERR_CUDA, cudaGetErrorString(e)); }
     if (stream) {
         c->stream = (cudaStream_t)stream;
     } else {
@@ -583,6 +600,7 @@ cvg_status cvg_context_destroy(cvg_context ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (auto &kv : ctx->libs) cudaLibraryUnload(kv.second);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     delete ctx;
     return CVG_OK;
 }
@@ -688,6 +706,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->iteration, sizeof(cvg_u32)},
         {(void **)&r->status, sizeof(cvg_u32)},
         {(void **)&r->scale_exp, sizeof(int)},
+        {(void **)&r->done, 2 * sizeof(cvg_u32)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
     };
@@ -711,6 +730,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaEventCreate(&r->ev1));
     r->ev0_own = r->ev0;
     r->ev1_own = r->ev1;
+    CK(cudaEventCreateWithFlags(&r->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&r->ev_join, cudaEventDisableTiming));
     // uniform grid x_j = j/N (src/main.cu:432-441)
     std::vector<double> xe((size_t)D * (N + 1));
     const double step = 1.0 / N;
@@ -725,6 +746,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->acc, 0, sizeof(cvg_acc_dev), st));
     CK(cudaMemsetAsync(r->iteration, 0, sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->status, 0, sizeof(cvg_u32), st));
+    CK(cudaMemsetAsync(r->done, 0, 2 * sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->stats, 0, sizeof(double) * 3 * p.max_it, st));
     CK(cudaMemsetAsync(r->grad, 0, sizeof(double) * std::max(1, f->n_params), st));
     if (f->n_params > 0)
@@ -750,6 +772,8 @@ cvg_status cvg_run_destroy(cvg_run r)
     for (auto &pr : r->fill_ev) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
     if (r->ev0_own) cudaEventDestroy(r->ev0_own);
     if (r->ev1_own) cudaEventDestroy(r->ev1_own);
+    if (r->ev_fork) cudaEventDestroy(r->ev_fork);
+    if (r->ev_join) cudaEventDestroy(r->ev_join);
     if (r->ubuf) cudaFree(r->ubuf);
     if (r->arena) cudaFree(r->arena);
     delete r;
@@ -1072,7 +1096,7 @@ cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int
     std::string all;
     cvg_status st = CVG_OK;
     for (int g = 0; g <= (has_grad ? 1 : 0) && st == CVG_OK; ++g) {
-        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi};
+        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi, 1024};
         std::vector<char> cubin;
         std::string l;
         st = nvrtc_cubin(make_source(f, k), nvrtc_options(arch), cubin, l);

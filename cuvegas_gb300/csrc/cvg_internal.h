@@ -14,6 +14,7 @@
 struct cvg_context_s {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;   // second stream: refinement runs beside the reallocation
     bool own_stream = false;
     int n_sm = 0;
     int smem_optin = 0;

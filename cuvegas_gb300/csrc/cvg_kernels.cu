@@ -127,6 +127,23 @@ __device__ __forceinline__ dfloat df_add(dfloat a, dfloat b)
     return r;
 }
 
+// Ticket of a finished block: true in the last of `nb` blocks (which then
+// resets the counter).  Writes of every block are visible to the last one.
+__device__ __forceinline__ bool last_block(cvg_u32 *ctr, unsigned nb)
+{
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const cvg_u32 t = atomicAdd(ctr, 1u);
+        last = (t == nb - 1);
+        if (last) *ctr = 0u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
 __device__ __forceinline__ void k3_results_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double scratch[3 * 32];
@@ -160,7 +177,15 @@ __device__ __forceinline__ void k3_results_dev(const cvg_realloc_args &a, const 
     }
 }
 
-__global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a) { k3_results_dev(a, blockIdx.x); }
+__device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb);
+__device__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb);
+
+__global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
+{
+    k3_results_dev(a, blockIdx.x);
+    const unsigned nb = cvg_realloc_blocks(a.n_cubes);
+    if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
+}
 
 
 // FP32 form of k3_results.  Per cube, with m = JF/n and q = JF2/n held as
@@ -259,10 +284,15 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
     }
 }
 
-__global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a) { k3_results_f32_dev(a, blockIdx.x); }
+__global__ void __launch_bounds__(RB) k3_results_f32(cvg_realloc_args a)
+{
+    k3_results_f32_dev(a, blockIdx.x);
+    const unsigned nb = cvg_realloc_blocks(a.n_cubes);
+    if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
+}
 
 
-__device__ __forceinline__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
+__device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
 {
     __shared__ double scratch[4 * 32];
     double v[4] = {0.0, 0.0, 0.0, 0.0};
@@ -313,7 +343,7 @@ __device__ __forceinline__ void k3_finish_dev(const cvg_realloc_args &a, unsigne
     }
 }
 
-__global__ void __launch_bounds__(1024) k3_finish(cvg_realloc_args a, unsigned nb) { k3_finish_dev(a, nb); }
+
 
 
 // mode 0: nh from the damped variances (updateNh, src/main.cu:173-187)
@@ -367,10 +397,15 @@ __device__ __forceinline__ void k3_count_dev(const cvg_realloc_args &a, int mode
     }
 }
 
-__global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode) { k3_count_dev(a, mode, blockIdx.x); }
+__global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)
+{
+    k3_count_dev(a, mode, blockIdx.x);
+    const unsigned nb = cvg_realloc_blocks(a.n_cubes);
+    if (last_block(&a.done[1], nb)) k3_scan_dev(a, nb);
+}
 
 
-__device__ __forceinline__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb)
+__device__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb)
 {
     __shared__ cvg_u64 scratch[33];
     const unsigned per = (nb + blockDim.x - 1) / blockDim.x;
@@ -385,7 +420,7 @@ __device__ __forceinline__ void k3_scan_dev(const cvg_realloc_args &a, unsigned 
     if (threadIdx.x == 0) a.bsums[nb] = total;
 }
 
-__global__ void __launch_bounds__(1024) k3_scan(cvg_realloc_args a, unsigned nb) { k3_scan_dev(a, nb); }
+
 
 
 __device__ __forceinline__ void k3_apply_dev(const cvg_realloc_args &a, unsigned nb, const unsigned blk)
@@ -594,13 +629,11 @@ __global__ void __launch_bounds__(RB) k3_results_b(cvg_realloc_batch B)
     const cvg_realloc_args a = B.A[i];
     if (a.fast_pow) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
     else k3_results_dev(a, blockIdx.x - B.blk_base[i]);
+    const unsigned nb = B.blk_base[i + 1] - B.blk_base[i];
+    if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
 }
 
-__global__ void __launch_bounds__(1024) k3_finish_b(cvg_realloc_batch B)
-{
-    const cvg_realloc_args a = B.A[blockIdx.x];
-    k3_finish_dev(a, cvg_realloc_blocks(a.n_cubes));
-}
+
 
 __global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
 {
@@ -608,14 +641,11 @@ __global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
     const cvg_realloc_args a = B.A[i];
     if (!a.adapt && mode != 1) return;
     k3_count_dev(a, mode == 0 ? (a.fast_pow ? 2 : 0) : mode, blockIdx.x - B.blk_base[i]);
+    const unsigned nb = B.blk_base[i + 1] - B.blk_base[i];
+    if (last_block(&a.done[1], nb)) k3_scan_dev(a, nb);
 }
 
-__global__ void __launch_bounds__(1024) k3_scan_b(cvg_realloc_batch B, int mode)
-{
-    const cvg_realloc_args a = B.A[blockIdx.x];
-    if (!a.adapt && mode != 1) return;
-    k3_scan_dev(a, cvg_realloc_blocks(a.n_cubes));
-}
+
 
 __global__ void __launch_bounds__(RB) k3_apply_b(cvg_realloc_batch B, int mode)
 {
@@ -718,12 +748,10 @@ cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cuda
 cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s)
 {
     const unsigned nb = cvg_realloc_blocks(a.n_cubes);
-    if (a.fast_pow) k3_results_f32<<<nb, RB, 0, s>>>(a);
+    if (a.fast_pow) k3_results_f32<<<nb, RB, 0, s>>>(a);   // + finish in the last block
     else k3_results<<<nb, RB, 0, s>>>(a);
-    k3_finish<<<1, 1024, 0, s>>>(a, nb);
     if (a.adapt) {
-        k3_count<<<nb, RB, 0, s>>>(a, a.fast_pow ? 2 : 0);
-        k3_scan<<<1, 1024, 0, s>>>(a, nb);
+        k3_count<<<nb, RB, 0, s>>>(a, a.fast_pow ? 2 : 0);    // + scan in the last block
         k3_apply<<<nb, RB, 0, s>>>(a, nb);
     }
     return cudaGetLastError();
@@ -738,7 +766,6 @@ cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cuda
         if (e != cudaSuccess) return e;
     }
     k3_count<<<nb, RB, 0, s>>>(a, 1);
-    k3_scan<<<1, 1024, 0, s>>>(a, nb);
     k3_apply<<<nb, RB, 0, s>>>(a, nb);
     return cudaGetLastError();
 }
@@ -776,11 +803,9 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
                                      cvg_u64 *tile_base, cudaStream_t s)
 {
     (void)fast;
-    k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);
-    k3_finish_b<<<B.n, 1024, 0, s>>>(B);
+    k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);          // + finish per instance
     if (adapt) {
-        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
-        k3_scan_b<<<B.n, 1024, 0, s>>>(B, 0);
+        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);      // + scan per instance
         k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
     }
     k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
@@ -790,7 +815,6 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
 cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_base, cudaStream_t s)
 {
     k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
-    k3_scan_b<<<B.n, 1024, 0, s>>>(B, 1);
     k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
     k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
     return cudaGetLastError();

@@ -35,6 +35,8 @@ struct cvg_realloc_args {
     cvg_u32 *iteration;
     cvg_u32 *status;
     int *scale_exp;         // FP32 form: scale exponent k of the fill (updated here); may be null
+    cvg_u32 *done;          // [2] block tickets (zero between launches): the last block of
+                            // the results / count kernels also runs the finish / scan step
     cvg_u64 max_tiles;
     cvg_i64 n_eval_it;
     double v_cubes;

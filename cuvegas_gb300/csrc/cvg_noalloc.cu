@@ -99,6 +99,7 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
     a.iteration = (cvg_u32 *)(b + kOffIt);
     a.status = (cvg_u32 *)(b + kOffStatus);
     a.scale_exp = nullptr;               // JF/JF2 are taken at their own magnitude
+    a.done = (cvg_u32 *)(b + kOffIt + 64);   // block tickets (cleared below)
     a.stats = est;                       // est[0] = I, est[1] = sigma^2, est[2] = samples
     a.tile_cube = tile_cube;
     a.max_tiles = tile_cube ? max_tiles : 0;

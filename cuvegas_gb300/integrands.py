@@ -8,7 +8,8 @@ prelude defines.
 Workloads (seeded synthetic inputs with the shapes of the benchmark configs):
   gauss      prod_d exp(-((x_d-0.5)/0.1)^2)/(0.1 sqrt(pi)), d = 4 or 8
   mixture    sum_{k=1,2} w_k prod_d exp(-((x_d-mu_kd)/s_k)^2), d = 6, 16 parameters
-  prodpeak   prod_d 1/(c_d^-2 + (x_d-u_d)^2), c ~ U(5,25), u ~ U(0,1)
+  prodpeak   prod_d 1/(c_d^-2 + (x_d-u_d)^2), c ~ U(5,25), u ~ U(0,1);
+             parameters theta = [c^-2, u] (prodpeak_theta)
   corner     (1 + sum_d c_d x_d)^-(d+1), c ~ U(0.1,1.0), d = 16
 """
 import numpy as np
@@ -68,13 +69,13 @@ __device__ void integrand_grad(float* x, const float* th, float* g) { cvg_mix_gr
 """
 
 PRODPEAK = r"""
-// theta = [c(d), u(d)]: prod_d 1/(c_d^-2 + (x_d-u_d)^2)
+// theta = [c^-2 (d), u(d)] (see prodpeak_theta): prod_d 1/(c_d^-2 + (x_d-u_d)^2)
 template <typename T> __device__ __forceinline__ T cvg_pp(T* x, const T* th) {
     T den = (T)1;
 #pragma unroll
     for (int d = 0; d < cvg_n_dim; ++d) {
-        const T c = th[d], a = x[d] - th[cvg_n_dim + d];
-        den *= (T)1 / (c * c) + a * a;
+        const T a = x[d] - th[cvg_n_dim + d];
+        den *= th[d] + a * a;
     }
     return (T)1 / den;
 }
@@ -120,6 +121,13 @@ def corner_theta(seed=0, dim=16):
     return rng.uniform(0.1, 1.0, size=dim)
 
 
+def prodpeak_theta(c, u):
+    """Parameters of PRODPEAK: [c^-2, u] (the reciprocal is taken once here,
+    not per sample)."""
+    c = np.asarray(c, dtype=np.float64)
+    return np.concatenate([1.0 / (c * c), np.asarray(u, dtype=np.float64)])
+
+
 def batch_instances(seed=0, n=512):
     """Batched product-peak family: dim ~ U{2..12}, evals/iteration
     log-uniform in [1e4, 1e7], c ~ U(5,25), u ~ U(0,1) per dimension."""
@@ -130,5 +138,5 @@ def batch_instances(seed=0, n=512):
         n_it = int(10 ** rng.uniform(4, 7))
         c = rng.uniform(5, 25, size=d)
         u = rng.uniform(0, 1, size=d)
-        out.append(dict(dim=d, n_eval_it=n_it, theta=np.concatenate([c, u])))
+        out.append(dict(dim=d, n_eval_it=n_it, c=c, u=u, theta=prodpeak_theta(c, u)))
     return out

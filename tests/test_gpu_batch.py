@@ -19,8 +19,8 @@ def _instances(n, seed, lo=4, hi=5):
         d = 2 + i % 11
         c = rng.uniform(5, 25, size=d)
         u = rng.uniform(0, 1, size=d)
-        out.append(dict(dim=d, n_eval_it=int(10 ** rng.uniform(lo, hi)),
-                        theta=np.concatenate([c, u])))
+        out.append(dict(dim=d, n_eval_it=int(10 ** rng.uniform(lo, hi)), c=c, u=u,
+                        theta=I.prodpeak_theta(c, u)))
     return out
 
 
@@ -56,8 +56,7 @@ def test_batch_fp32_family_against_analytic(ctx):
         res, _, _ = b.results()
     pulls = []
     for i, inst in enumerate(insts):
-        d, th = inst["dim"], inst["theta"]
-        exact = A.product_peak(th[:d], th[d:])
+        exact = A.product_peak(inst["c"], inst["u"])
         pulls.append((res[i].result - exact) / res[i].error)
         assert np.isfinite(res[i].chi2_dof)
     pulls = np.abs(np.array(pulls))

@@ -43,5 +43,5 @@ def test_c4_product_peak_instances(ctx):
         d, th = inst["dim"], inst["theta"]
         res, _, _ = _run(ctx, I.PRODPEAK, d, max(inst["n_eval_it"], 10000), 10, L.PREC_FP32,
                          theta=th, P=2 * d)
-        exact = A.product_peak(th[:d], th[d:])
+        exact = A.product_peak(inst["c"], inst["u"])
         assert abs(res.result - exact) < 5 * res.error, (d, res.result, exact, res.error)
