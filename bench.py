@@ -217,8 +217,8 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from cuvegas_gb300 import _build, _lib as L, runtime, integrands as I
-    from oracle import analytic as A
+    from cuvegas_gb300 import _build, _lib as L, replicas, runtime, integrands as I
+    from cuvegas_gb300 import analytic as A
     _build.build()
     stream = torch.cuda.Stream(device=local)
     ctx = runtime.Context(local, stream=C_stream(stream))
@@ -235,7 +235,7 @@ def run_ours(args):
     def measure(prec, n_it):
         p = runtime.make_params(DIM, n_it * (warm + steps), warm + steps, skip=min(skip, warm + steps - 1),
                                 n_intervals=NBINS, seed=SEED + rank, precision=prec,
-                                flags=L.FLAG_TIME_FILL, instance=rank)
+                                flags=L.FLAG_TIME_FILL, instance=replicas.instance_id(rank))
         with runtime.Run(f, p) as r:
             r.iterate(warm)
             r.sync()
@@ -272,15 +272,8 @@ def run_ours(args):
             r.sync()
 
     chosen = measure(L.PREC_FP32, N_IT)
-    # max over ranks of the timed region
-    ms_all = chosen["ms"]
-    ev_all = chosen["evals"]
-    if world > 1:
-        t = torch.tensor([ms_all, ev_all], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        ms_all, ev_all = float(mx[0]), float(t[1])
+    # slowest rank's timed region, all ranks' evaluations
+    ms_all, ev_all = replicas.reduce_timing(chosen["ms"], chosen["evals"], device="cuda")
     value = ev_all / (ms_all / 1e3)
 
     extra = {}
@@ -362,8 +355,8 @@ def run_workload(args):
     """Lines for the other benchmark configurations (one JSON line each)."""
     import numpy as np
     import torch
-    from cuvegas_gb300 import _build, _lib as L, runtime, integrands as I
-    from oracle import analytic as A
+    from cuvegas_gb300 import _build, _lib as L, replicas, runtime, integrands as I
+    from cuvegas_gb300 import analytic as A
     _build.build()
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream(device=0)

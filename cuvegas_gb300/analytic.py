@@ -1,4 +1,4 @@
-"""Closed-form integrals over [0,1]^d of the benchmark integrands (checker only).
+"""Closed-form integrals over [0,1]^d of the benchmark integrand families, used to check estimates.
 
 - Gaussian, width s, centre m:  prod_d erf-difference; for m=0.5, s=0.1 the
   normalised form integrates to erf(5)^d.

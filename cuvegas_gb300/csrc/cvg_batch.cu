@@ -53,6 +53,8 @@ struct inst_host {
     float *x_edges32;
     cvg_u32 *counts, *nh_new, *tile_cube, *iteration;
     int *scale_exp;
+    double *scale_ss;
+    int *bin_exp;
     cvg_u32 *done;
     cvg_u64 *nh_sum, *bsums;
     cvg_acc_dev *acc;
@@ -86,6 +88,56 @@ struct cvg_batch_s {
 
 namespace {
 
+size_t seg(size_t bytes) { return (bytes + 255) & ~(size_t)255; }
+
+// Device buffers of one instance, in arena order.  With base == nullptr only
+// the offset advances (sizing pass); otherwise the pointers are set too.
+template <typename P> void place(P *&ptr, size_t bytes, char *base, size_t &off)
+{
+    if (base) ptr = (P *)(base + off);
+    off += seg(bytes);
+}
+
+void inst_layout(inst_host &h, int N, int max_it, char *base, size_t &off)
+{
+    const size_t D = (size_t)h.dim;
+    place(h.x_edges, sizeof(double) * D * (N + 1), base, off);
+    place(h.x_edges32, sizeof(float) * D * (N + 1), base, off);
+    place(h.weights, sizeof(double) * D * N, base, off);
+    place(h.counts, sizeof(cvg_u32) * D * N, base, off);
+    place(h.JF, sizeof(double) * h.n_cubes, base, off);
+    place(h.JF2, sizeof(double) * h.n_cubes, base, off);
+    place(h.dh, sizeof(double) * h.n_cubes, base, off);
+    place(h.nh_sum, sizeof(cvg_u64) * (h.n_cubes + 1ull), base, off);
+    place(h.nh_new, sizeof(cvg_u32) * h.n_cubes, base, off);
+    place(h.tile_cube, sizeof(cvg_u32) * h.max_tiles, base, off);
+    place(h.partials, sizeof(double) * 4 * h.nb, base, off);
+    place(h.bsums, sizeof(cvg_u64) * (h.nb + 1), base, off);
+    place(h.stats, sizeof(double) * 3 * max_it, base, off);
+    place(h.acc, sizeof(cvg_acc_dev), base, off);
+    place(h.iteration, 16, base, off);
+    place(h.scale_exp, 16, base, off);
+    place(h.scale_ss, 16, base, off);
+    place(h.done, 16, base, off);
+    place(h.bin_exp, sizeof(int) * (D * N + 1), base, off);
+    place(h.theta, sizeof(double) * std::max(1, h.n_params), base, off);
+    place(h.grad, sizeof(double) * std::max(1, h.n_params), base, off);
+}
+
+// Per-batch tables after the instances' buffers.
+void tables_layout(cvg_batch_s *b, char *base, size_t &off)
+{
+    const size_t n = (size_t)b->n;
+    place(b->d_status, 16, base, off);
+    place(b->d_fill, sizeof(cvg_fill_args) * n, base, off);
+    place(b->d_realloc, sizeof(cvg_realloc_args) * n, base, off);
+    place(b->d_refine, sizeof(cvg_refine_args) * n, base, off);
+    place(b->d_dims, sizeof(int) * n, base, off);
+    place(b->d_blk_base, sizeof(unsigned) * (n + 1), base, off);
+    place(b->d_dim_base, sizeof(unsigned) * (n + 1), base, off);
+    place(b->d_tile_base, sizeof(cvg_u64) * (n + 1), base, off);
+}
+
 std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
 {
     const char *T = b.p.precision == CVG_PREC_FP32 ? "float" : "double";
@@ -116,7 +168,7 @@ std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
                   "extern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_batch_entry("
                   "const cvg_batch_args b) { cvg_fill_batch<%s, %d, cvg_disp, %d>(b); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_batch_entry("
-                  "const cvg_batch_args b) { cvg_pilot_batch<%s, 8, cvg_disp>(b); }\n",
+                  "const cvg_batch_args b) { cvg_pilot_batch<%s, 32, cvg_disp>(b); }\n",
                   b.block, T, b.block, b.p.n_intervals, T);
     s += entry;
     return s;
@@ -172,6 +224,9 @@ cvg_status enqueue_iteration(cvg_batch_s *b, bool timed)
     return CVG_OK;
 }
 
+cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *theta,
+                      const std::set<int> &dims, size_t total);
+
 }  // namespace
 
 extern "C" {
@@ -210,7 +265,6 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     int dmax = 0, pmax = 0;
     b->inst.resize(n);
     size_t total = 0;
-    auto seg = [](size_t bytes) { return (bytes + 255) & ~(size_t)255; };
     for (int i = 0; i < n; ++i) {
         inst_host &h = b->inst[i];
         const cvg_instance &in = insts[i];
@@ -238,18 +292,9 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         dims.insert(h.dim);
         dmax = std::max(dmax, h.dim);
         pmax = std::max(pmax, h.n_params);
-        const int D = h.dim;
-        total += seg(sizeof(double) * D * (N + 1)) + seg(sizeof(float) * D * (N + 1)) +
-                 seg(sizeof(double) * D * N) + seg(sizeof(cvg_u32) * D * N) +
-                 3 * seg(sizeof(double) * h.n_cubes) + seg(sizeof(cvg_u64) * (h.n_cubes + 1ull)) +
-                 seg(sizeof(cvg_u32) * h.n_cubes) + seg(sizeof(cvg_u32) * h.max_tiles) +
-                 seg(sizeof(double) * 4 * h.nb) + seg(sizeof(cvg_u64) * (h.nb + 1)) +
-                 seg(sizeof(double) * 3 * p.max_it) + seg(sizeof(cvg_acc_dev)) + 3 * seg(16) +
-                 2 * seg(sizeof(double) * std::max(1, h.n_params));
+        inst_layout(h, N, p.max_it, nullptr, total);
     }
-    total += seg(sizeof(cvg_fill_args) * n) + seg(sizeof(cvg_realloc_args) * n) +
-             seg(sizeof(cvg_refine_args) * n) + seg(sizeof(int) * n) + 2 * seg(sizeof(unsigned) * (n + 1)) +
-             seg(sizeof(cvg_u64) * (n + 1)) + seg(16);
+    tables_layout(b, nullptr, total);
     const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8;
     b->fill_smem = cvg_fill_smem_bytes(dmax, N, tsz, 1, 1, 0, b->TS, pmax, b->block);
     if (b->fill_smem > (size_t)ctx->smem_optin) {
@@ -263,41 +308,46 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         delete b;
         return cvg_internal_fail(CVG_ERR_NOMEM, std::string("batch arena: ") + cudaGetErrorString(e));
     }
+    const cvg_status st_init = batch_init(b, insts, theta, dims, total);
+    if (st_init != CVG_OK) {
+        cvg_batch_destroy(b);
+        return st_init;
+    }
     *out = b;
+    return CVG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Second half of cvg_batch_create: lays out the arena, uploads the instances'
+// initial state and tables, compiles the fill and runs the FP32 pilot.  On
+// failure the caller destroys the half-built batch.
+cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *theta,
+                      const std::set<int> &dims, size_t total)
+{
+    const int n = b->n;
+    const cvg_params &p = b->p;
+    const int N = p.n_intervals;
+    cvg_context ctx = b->ctx;
     cudaStream_t st = ctx->stream;
     BCK(cudaMemsetAsync(b->arena, 0, total, st));
-    char *ptr = (char *)b->arena;
-    auto take = [&](size_t bytes) { char *q = ptr; ptr += seg(bytes); return q; };
+    char *base = (char *)b->arena;
+    size_t off = 0;
     std::vector<cvg_fill_args> hf(n);
     std::vector<cvg_realloc_args> hr(n);
     std::vector<cvg_refine_args> hq(n);
     std::vector<int> hdims(n);
     std::vector<unsigned> blk_base(n + 1), dim_base(n + 1);
     std::vector<double> xe;
-    b->d_status = (cvg_u32 *)take(16);
+    for (int i = 0; i < n; ++i) inst_layout(b->inst[i], N, p.max_it, base, off);
+    tables_layout(b, base, off);
+    if (off != total) return cvg_internal_fail(CVG_ERR_STATE, "batch arena layout mismatch");
     size_t th_off = 0;
     for (int i = 0; i < n; ++i) {
         inst_host &h = b->inst[i];
         const int D = h.dim;
-        h.x_edges = (double *)take(sizeof(double) * D * (N + 1));
-        h.x_edges32 = (float *)take(sizeof(float) * D * (N + 1));
-        h.weights = (double *)take(sizeof(double) * D * N);
-        h.counts = (cvg_u32 *)take(sizeof(cvg_u32) * D * N);
-        h.JF = (double *)take(sizeof(double) * h.n_cubes);
-        h.JF2 = (double *)take(sizeof(double) * h.n_cubes);
-        h.dh = (double *)take(sizeof(double) * h.n_cubes);
-        h.nh_sum = (cvg_u64 *)take(sizeof(cvg_u64) * (h.n_cubes + 1ull));
-        h.nh_new = (cvg_u32 *)take(sizeof(cvg_u32) * h.n_cubes);
-        h.tile_cube = (cvg_u32 *)take(sizeof(cvg_u32) * h.max_tiles);
-        h.partials = (double *)take(sizeof(double) * 4 * h.nb);
-        h.bsums = (cvg_u64 *)take(sizeof(cvg_u64) * (h.nb + 1));
-        h.stats = (double *)take(sizeof(double) * 3 * p.max_it);
-        h.acc = (cvg_acc_dev *)take(sizeof(cvg_acc_dev));
-        h.iteration = (cvg_u32 *)take(16);
-        h.scale_exp = (int *)take(16);
-        h.done = (cvg_u32 *)take(16);
-        h.theta = (double *)take(sizeof(double) * std::max(1, h.n_params));
-        h.grad = (double *)take(sizeof(double) * std::max(1, h.n_params));
         // uniform grid (src/main.cu:432-441)
         xe.resize((size_t)D * (N + 1));
         for (int d = 0; d < D; ++d)
@@ -324,6 +374,8 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         a.grad = h.grad;
         a.status = b->d_status;
         a.scale_exp = p.precision == CVG_PREC_FP32 ? h.scale_exp : nullptr;
+        a.scale_ss = p.precision == CVG_PREC_FP32 ? h.scale_ss : nullptr;
+        a.bin_exp = p.precision == CVG_PREC_FP32 ? h.bin_exp : nullptr;
         a.max_tiles = h.max_tiles;
         a.seed = p.seed;
         a.instance = insts[i].instance;
@@ -364,6 +416,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         q.x_edges32 = h.x_edges32;
         q.weights = h.weights;
         q.counts = h.counts;
+        q.bin_exp = a.bin_exp;
         q.alpha = p.alpha;
         q.dim = D;
         q.n_intervals = N;
@@ -374,13 +427,6 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     }
     b->total_blocks = blk_base[n];
     b->total_dims = dim_base[n];
-    b->d_fill = (cvg_fill_args *)take(sizeof(cvg_fill_args) * n);
-    b->d_realloc = (cvg_realloc_args *)take(sizeof(cvg_realloc_args) * n);
-    b->d_refine = (cvg_refine_args *)take(sizeof(cvg_refine_args) * n);
-    b->d_dims = (int *)take(sizeof(int) * n);
-    b->d_blk_base = (unsigned *)take(sizeof(unsigned) * (n + 1));
-    b->d_dim_base = (unsigned *)take(sizeof(unsigned) * (n + 1));
-    b->d_tile_base = (cvg_u64 *)take(sizeof(cvg_u64) * (n + 1));
     BCK(cudaMemcpyAsync(b->d_fill, hf.data(), sizeof(cvg_fill_args) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_realloc, hr.data(), sizeof(cvg_realloc_args) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_refine, hq.data(), sizeof(cvg_refine_args) * n, cudaMemcpyHostToDevice, st));
@@ -407,22 +453,35 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     // FP32 form: per-instance scale exponent from a pilot evaluation
     if (p.precision == CVG_PREC_FP32) {
         std::vector<int> ex(n, -1000);
-        for (int i = 0; i < n; ++i)
+        std::vector<double> ss(n, 0.0);
+        for (int i = 0; i < n; ++i) {
             BCK(cudaMemcpyAsync(b->inst[i].scale_exp, &ex[i], sizeof(int), cudaMemcpyHostToDevice, st));
+            BCK(cudaMemsetAsync(b->inst[i].scale_ss, 0, sizeof(double), st));
+        }
         cvg_batch_args ba = batch_args(b);
         void *args[] = {&ba};
-        BCK(cudaLaunchKernel((const void *)b->pilot, dim3(8 * n), dim3(256), args, 0, st));
-        for (int i = 0; i < n; ++i)
+        BCK(cudaLaunchKernel((const void *)b->pilot, dim3(32 * n), dim3(256), args, 0, st));
+        // the pilot's bin histograms -> first per-bin exponent tables (grids kept)
+        cvg_refine_batch rb = refine_batch(b);
+        rb.keep_grid = 1;
+        BCK(cvg_launch_refine_batch(rb, N, st));
+        for (int i = 0; i < n; ++i) {
             BCK(cudaMemcpyAsync(&ex[i], b->inst[i].scale_exp, sizeof(int), cudaMemcpyDeviceToHost, st));
+            BCK(cudaMemcpyAsync(&ss[i], b->inst[i].scale_ss, sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
         BCK(cudaStreamSynchronize(st));
         for (int i = 0; i < n; ++i) {
-            ex[i] = ex[i] < -100 ? 0 : std::min(ex[i], 100);
+            ex[i] = cvg_internal_pilot_scale(ex[i], ss[i], 32.0 * 256.0);
             BCK(cudaMemcpyAsync(b->inst[i].scale_exp, &ex[i], sizeof(int), cudaMemcpyHostToDevice, st));
         }
     }
     BCK(cudaStreamSynchronize(st));
     return CVG_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 cvg_status cvg_batch_destroy(cvg_batch b)
 {

@@ -36,6 +36,10 @@ struct cvg_fill_args {
     double *grad;                 // [n_params] dI/dtheta accumulator (gradient pass)
     cvg_u32 *status;              // error bits
     int *scale_exp;               // FP32 form: f*jac is scaled by 2^-scale_exp (may be null)
+    double *scale_ss;             // FP32-form pilot: sum of (f*jac)^2 over its samples
+    int *bin_exp;                 // FP32 form: [dim][N] binary exponent of each bin's expected
+                                  // per-sample (f*jac)^2 (unscaled); [dim*N] = the scale
+                                  // exponent k of the last fill (null for FP64)
     cvg_u64 max_tiles;            // capacity of tile_cube
     cvg_u64 seed;                 // Philox key
     cvg_u32 instance;             // Philox counter word 3, bits 8..31

@@ -115,6 +115,79 @@ CVG_D int cvg_bin(double z, int N, double, double &frac)
     return b;
 }
 
+// Per-bin histogram update in shared memory.
+//
+// FP32 form: shared-memory float atomics are not a single native operation
+// on this GPU (measured: float adds to shared memory run at a quarter of the
+// u32 rate), so the bin's Sum (f*jac)^2 is kept in fixed point in a u32 word
+// and updated with the native integer atomic.  Each bin has its own scale:
+// the top 8 bits of its count word hold a signed exponent e (set when the
+// histogram is cleared; counts stay below 2^24 between flushes), and a weight
+// w is added as round(w * 2^(16-e)) units.  e comes from the bin's expected
+// per-sample weight, so every bin -- also one whose weights are 1e-12 of the
+// core's -- is resolved to about 2^-16 of its typical sample.  A word that
+// wraps adds its 2^32 units to the global FP64 sum; a weight at or above
+// 2^(e+7) (or non-finite) goes to the global FP64 sum directly.
+// FP64 form: FP64 atomics, sums in the reference's precision.
+#define CVG_HIST_CNT_MASK 0x00FFFFFFu
+#define CVG_HIST_MAX_RUN 0x00FFF000u   // samples between flushes (counts < 2^24)
+// Fixed-point bin sums are used by the FP32 form up to this dimension;
+// above it the shared-memory float atomics are kept.
+#ifndef CVG_HIST_FIX_MAX_DIM
+#define CVG_HIST_FIX_MAX_DIM 16
+#endif
+template <int D, typename T> CVG_D constexpr bool cvg_hist_fixed()
+{
+    return sizeof(T) == 4 && D <= CVG_HIST_FIX_MAX_DIM;
+}
+
+template <bool FIX>
+CVG_D void cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
+{
+    if (!FIX) {
+        atomicAdd(hw + i, w);
+        atomicAdd(hc + i, 1u);
+        return;
+    }
+    const cvg_u32 old = atomicAdd(hc + i, 1u);
+    const int e = (int)old >> 24;                             // this bin's scale exponent
+    const float s = w * __int_as_float((143 - e) << 23);      // w * 2^(16-e)
+    if (s < 8388608.0f) {   // round-to-nearest integer by a 2^23 add (no conversion instruction)
+        const cvg_u32 q = __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u;
+        const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
+        if (o + q < o) atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
+    } else {
+        atomicAdd(gw + i, cvg_f2d(w));
+    }
+}
+template <bool FIX>
+CVG_D void cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
+{
+    atomicAdd(hw + i, w);
+    atomicAdd(hc + i, 1u);
+}
+// Bin sum and count of a shared-memory histogram entry, in the units of the
+// global histogram.
+template <bool FIX>
+CVG_D double cvg_hist_value(const float *hw, const cvg_u32 *hc, int i)
+{
+    if (!FIX) return cvg_f2d(hw[i]);
+    return ldexp((double)reinterpret_cast<const cvg_u32 *>(hw)[i], ((int)hc[i] >> 24) - 16);
+}
+template <bool FIX>
+CVG_D double cvg_hist_value(const double *hw, const cvg_u32 *, int i) { return hw[i]; }
+template <bool FIX> CVG_D cvg_u32 cvg_hist_count(cvg_u32 w) { return FIX ? (w & CVG_HIST_CNT_MASK) : w; }
+// Cleared count word of bin i: with fixed point it carries the bin's scale
+// exponent (unscaled exponent from the table minus 2k for the f*jac scaling).
+template <bool FIX>
+CVG_D cvg_u32 cvg_hist_word(const cvg_fill_args &a, int i, int kx)
+{
+    if (!FIX) return 0u;
+    int e = a.bin_exp ? a.bin_exp[i] - 2 * kx : 0;
+    e = e < -100 ? -100 : (e > 100 ? 100 : e);
+    return (cvg_u32)e << 24;
+}
+
 // Stratum offsets coord_d * dy of cube c (digit d of c in base n_strat, least
 // significant first: src/main.cu:43-47); cvg_cube_next steps to cube c+1
 // like an odometer.
@@ -192,8 +265,6 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
         for (int i = tid; i < P; i += BS) sm.th[i] = (T)a.theta[i];
     if (ESM)
         for (int i = tid; i < D * (N + 1); i += BS) sm.E[i] = grid[i];
-    if (H)
-        for (int i = tid; i < D * N; i += BS) { sm.hw[i] = (T)0; sm.hc[i] = 0u; }
     cx.G = ESM ? sm.E : grid;
     cx.it = *a.iteration;
     cx.k0 = (cvg_u32)a.seed;
@@ -209,6 +280,16 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     // sums are widened back with the exponent shift (exact)
     cx.kx = (sizeof(T) == 4 && a.scale_exp) ? *a.scale_exp : 0;
     cx.jac0 = cvg_scale_pow2((T)0, cx.kx);
+    if (H) {
+        for (int i = tid; i < D * N; i += BS) {
+            sm.hw[i] = (T)0;
+            sm.hc[i] = cvg_hist_word<cvg_hist_fixed<D, T>()>(a, i, cx.kx);
+        }
+        // the refinement turns this fill's bin sums (units 2^-2k) back into
+        // unscaled exponents for the next fill's table
+        // (every CTA of the instance writes the same value)
+        if (sizeof(T) == 4 && a.bin_exp && tid == 0) a.bin_exp[D * N] = cx.kx;
+    }
 }
 
 // One tile: samples [tile*TS, min((tile+1)*TS, S)).  Returns false (and sets a
@@ -330,8 +411,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
                     if (H) {
-                        atomicAdd(&sm.hw[d * N + bin[d]], jf2);
-                        atomicAdd(&sm.hc[d * N + bin[d]], 1u);
+                        cvg_hist_add<cvg_hist_fixed<D, T>()>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
                     } else {
                         atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
                         atomicAdd(&a.counts[d * N + bin[d]], 1u);
@@ -359,18 +439,22 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
     return true;
 }
 
-// Add the CTA's shared-memory bin histograms to the global FP64/u32 ones.
+// Add the CTA's shared-memory bin histograms to the global FP64/u32 ones;
+// with reset, clear them for more samples (scale exponents kept).
 template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD, int NI>
-CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm)
+CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
+                          bool reset = false)
 {
     if (!(HSM && !GRAD)) return;
     __syncthreads();
     const int N = NI > 0 ? NI : a.n_intervals;
     for (int i = threadIdx.x; i < D * N; i += BS) {
-        const cvg_u32 cn = sm.hc[i];
+        const cvg_u32 cn = cvg_hist_count<cvg_hist_fixed<D, T>()>(sm.hc[i]);
         if (cn) {
-            atomicAdd(&a.weights[i], cvg_to_double(sm.hw[i]));
+            const double w = cvg_hist_value<cvg_hist_fixed<D, T>()>(sm.hw, sm.hc, i);
+            if (w != 0.0) atomicAdd(&a.weights[i], w);
             atomicAdd(&a.counts[i], cn);
+            if (reset) { sm.hw[i] = (T)0; sm.hc[i] -= cn; }
         }
     }
     __syncthreads();
@@ -403,10 +487,17 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     for (int p = 0; p < PP; ++p) gacc[p].reset();
     __syncthreads();
 
-    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x)
+    cvg_u64 since = 0;   // samples in the shared histograms since their last flush
+    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        if (since + (cvg_u64)TS > CVG_HIST_MAX_RUN) {
+            cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI>(a, sm, true);
+            since = 0;
+        }
+        since += (cvg_u64)TS;
         if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI>(a, sm, cx, tile, n_tiles, S,
                                                                       gacc))
             break;
+    }
 
     cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI>(a, sm);
     if (GRAD) {
@@ -469,20 +560,33 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
             __syncthreads();
             const cvg_u64 S = a.nh_sum[a.n_cubes];
             const cvg_u64 nt = b.tile_base[i + 1] - tb;
-            for (cvg_u64 lt = t - tb; lt < te - tb; ++lt)
+            cvg_u64 since = 0;
+            for (cvg_u64 lt = t - tb; lt < te - tb; ++lt) {
+                if (since + (cvg_u64)a.tile_samples > CVG_HIST_MAX_RUN) {
+                    cvg_fill_flush<D, T, BS, true, true, P, false, NI>(a, sm, true);
+                    since = 0;
+                }
+                since += (cvg_u64)a.tile_samples;
                 if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI>(a, sm, cx, lt, nt,
                                                                                  S, nullptr))
                     break;
+            }
             cvg_fill_flush<D, T, BS, true, true, P, false, NI>(a, sm);
         });
         t = te;
     }
 }
 
-// Pilot for the FP32 form's scale: the binary exponent of max |f*jac| over
-// one sample in each of the first cubes (grid as it is now, Philox counter
-// word 2 = 0xFFFFFFFF so no iteration's samples are reused).  Results are
-// combined with atomicMax into *a.scale_exp (initialised by the host).
+// Pilot for the FP32 form's scales: samples uniform in [0,1)^dim mapped
+// through the grid as it is now (Philox counter word 2 = 0xFFFFFFFF, so no
+// iteration's samples are reused).  It takes the binary exponent of max
+// |f*jac| (atomicMax into *a.scale_exp, initialised by the host) and the sum
+// of (f*jac)^2 in FP64 (atomicAdd into *a.scale_ss, zeroed by the host), from
+// which the host sets 2^k near the rms of f*jac, raised where needed so that
+// the largest (f*jac*2^-k)^2 stays in FP32 range.  With a.bin_exp it also adds
+// each sample's unscaled (f*jac)^2 and count to the global bin histograms
+// (zero beforehand); the refinement kernel, run without adaptation, turns
+// them into the first fill's per-bin exponents.
 template <int D, typename T, int BS, int P, class F>
 CVG_D void cvg_pilot_body(const cvg_fill_args &a, cvg_u32 blk)
 {
@@ -490,42 +594,58 @@ CVG_D void cvg_pilot_body(const cvg_fill_args &a, cvg_u32 blk)
     for (int i = threadIdx.x; i < P; i += BS) th[i] = (T)a.theta[i];
     __syncthreads();
     const cvg_u32 gid = blk * BS + threadIdx.x;
-    const cvg_u32 c = gid % a.n_cubes;
-    const cvg_u32 j = gid / a.n_cubes;
-    const int N = a.n_intervals, ns = a.n_strat;
-    const T dy = (T)1 / (T)ns, fN = (T)N, fNm1 = (T)(N - 1);
+    const int N = a.n_intervals;
+    const T fN = (T)N, fNm1 = (T)(N - 1);
     const T *grid = cvg_grid_src<T>::get(a);
-    int coord[D];
-    T cdy[D];
-    cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
     constexpr int NB = (D + 3) / 4;
     cvg_u32 rr[NB * 4];
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-        const cvg_u32x4 r4 = cvg_philox(j, c, 0xFFFFFFFFu, (cvg_u32)b | (a.instance << 8),
+        const cvg_u32x4 r4 = cvg_philox(0u, gid, 0xFFFFFFFFu, (cvg_u32)b | (a.instance << 8),
                                         (cvg_u32)a.seed, (cvg_u32)(a.seed >> 32));
         rr[4 * b + 0] = r4.x; rr[4 * b + 1] = r4.y; rr[4 * b + 2] = r4.z; rr[4 * b + 3] = r4.w;
     }
     T x[D];
+    int bin[D];
     T jac = (T)1;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-        const T y = cvg_fma(cvg_uniform<T>(rr[d]), dy, cdy[d]);
-        const T z = y * fN;
+        const T z = cvg_uniform<T>(rr[d]) * fN;
         T frac;
         const int b = cvg_bin(z, N, fNm1, frac);
         const T e0 = grid[d * (N + 1) + b], dx = grid[d * (N + 1) + b + 1] - e0;
         x[d] = cvg_fma(dx, frac, e0);
         jac *= fN * dx;
+        bin[d] = b;
     }
     const T v = (T)F::f(x, th) * jac;
     const float fv = fabsf((float)v);
     int e = -200;
-    if (fv > 0.f && fv <= 3.4e38f) e = (int)((__float_as_uint(fv) >> 23) & 0xFFu) - 127;
-    else if (!(fv <= 3.4e38f)) e = 128;
+    double sq = 0.0;
+    if (fv > 0.f && fv <= 3.4e38f) {
+        e = (int)((__float_as_uint(fv) >> 23) & 0xFFu) - 127;
+        const double vd = cvg_to_double(v < (T)0 ? -v : v);
+        sq = vd * vd;
+    } else if (!(fv <= 3.4e38f)) {
+        e = 128;
+    }
+    if (a.bin_exp && fv <= 3.4e38f) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(a.scale_exp, e);
+        for (int d = 0; d < D; ++d) {
+            atomicAdd(&a.weights[d * N + bin[d]], sq);
+            atomicAdd(&a.counts[d * N + bin[d]], 1u);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        e = max(e, __shfl_down_sync(0xffffffffu, e, o));
+        sq += __shfl_down_sync(0xffffffffu, sq, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(a.scale_exp, e);
+        if (a.scale_ss) atomicAdd(a.scale_ss, sq);
+    }
+    if (a.bin_exp && blk == 0 && threadIdx.x == 0) a.bin_exp[D * N] = 0;   // sums are unscaled
 }
 
 // Batched pilot: blocks [i*PB, (i+1)*PB) evaluate instance i.

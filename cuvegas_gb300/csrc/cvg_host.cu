@@ -105,6 +105,8 @@ struct cvg_run_s {
     cvg_u32 *counts = nullptr, *nh_new = nullptr, *tile_cube = nullptr, *iteration = nullptr;
     cvg_u32 *status = nullptr;
     int *scale_exp = nullptr;
+    double *scale_ss = nullptr;
+    int *bin_exp = nullptr;
     cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
@@ -374,6 +376,7 @@ cvg_refine_args refine_args(cvg_run_s *r)
     a.x_edges32 = r->x_edges32;
     a.weights = r->weights;
     a.counts = r->counts;
+    a.bin_exp = r->p.precision == CVG_PREC_FP32 ? r->bin_exp : nullptr;
     a.alpha = r->p.alpha;
     a.dim = r->f->dim;
     a.n_intervals = r->p.n_intervals;
@@ -398,6 +401,8 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.grad = r->grad;
     a.status = r->status;
     a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
+    a.scale_ss = r->p.precision == CVG_PREC_FP32 ? r->scale_ss : nullptr;
+    a.bin_exp = r->p.precision == CVG_PREC_FP32 ? r->bin_exp : nullptr;
     a.max_tiles = r->max_tiles;
     a.seed = r->p.seed;
     a.instance = r->p.instance;
@@ -447,15 +452,22 @@ cvg_status run_pilot(cvg_run_s *r)
     const int init = -1000;
     cudaStream_t st = r->ctx->stream;
     CK(cudaMemcpyAsync(r->scale_exp, &init, sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(r->scale_ss, 0, sizeof(double), st));
     cvg_fill_args a = fill_args(r);
     void *args[] = {&a};
-    const cvg_u64 pts = std::min<cvg_u64>((cvg_u64)r->ctx->n_sm * 1024, 4ull * r->n_cubes + 255);
+    const cvg_u64 pts = (cvg_u64)r->ctx->n_sm * 1024;   // ~150 samples per bin at 1024 bins
     const unsigned blocks = (unsigned)((pts + 255) / 256);
     CK(cudaLaunchKernel((const void *)r->fill.pilot, dim3(blocks), dim3(256), args, 0, st));
+    // the pilot's bin histograms -> the first fill's per-bin exponents (grid kept)
+    cvg_refine_args q = refine_args(r);
+    q.adapt = 0;
+    CK(cvg_launch_refine(q, st));
     int e = 0;
+    double ss = 0.0;
     CK(cudaMemcpyAsync(&e, r->scale_exp, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&ss, r->scale_ss, sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    e = e < -100 ? 0 : (e > 100 ? 100 : e);   // no finite nonzero value seen: no scaling
+    e = cvg_internal_pilot_scale(e, ss, (double)blocks * 256.0);
     CK(cudaMemcpyAsync(r->scale_exp, &e, sizeof(int), cudaMemcpyHostToDevice, st));
     return CVG_OK;
 }
@@ -527,6 +539,19 @@ cvg_status cvg_internal_compile_only(const std::string &src, const char *arch, s
 const char *cvg_internal_src_common() { return cvg_src_common; }
 const char *cvg_internal_src_fill() { return cvg_src_fill; }
 double cvg_internal_now_ms() { return now_ms(); }
+
+int cvg_internal_pilot_scale(int emax, double ss, double n)
+{
+    if (emax < -100) return 0;                  // no finite nonzero value seen: no scaling
+    int k = emax;
+    const double ms = ss / n;
+    if (ms > 0.0 && std::isfinite(ms)) {
+        int e = 0;
+        std::frexp(ms, &e);
+        k = std::max(e / 2, emax - 60);
+    }
+    return std::min(std::max(k, -100), 100);
+}
 
 void cvg_internal_result(const double *stats, int max_it, int done, int skip, cvg_result *out)
 {
@@ -706,6 +731,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->iteration, sizeof(cvg_u32)},
         {(void **)&r->status, sizeof(cvg_u32)},
         {(void **)&r->scale_exp, sizeof(int)},
+        {(void **)&r->scale_ss, sizeof(double)},
+        {(void **)&r->bin_exp, sizeof(int) * ((size_t)D * N + 1)},
         {(void **)&r->done, 2 * sizeof(cvg_u32)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
@@ -723,8 +750,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         *s.ptr = (char *)r->arena + off;
         off += (s.bytes + 255) & ~(size_t)255;
     }
-    *out = r;   // from here on cvg_run_destroy cleans up
-
+    // initial state; on failure the half-built run is destroyed here
+    const cvg_status ist = [&]() -> cvg_status {
     cudaStream_t st = ctx->stream;
     CK(cudaEventCreate(&r->ev0));
     CK(cudaEventCreate(&r->ev1));
@@ -758,6 +785,13 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->scale_exp, 0, sizeof(int), st));
     if (p.precision == CVG_PREC_FP32) CKS(run_pilot(r));
     CK(cudaStreamSynchronize(st));
+    return CVG_OK;
+    }();
+    if (ist != CVG_OK) {
+        cvg_run_destroy(r);
+        return ist;
+    }
+    *out = r;
     return CVG_OK;
 }
 
@@ -899,6 +933,7 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     case CVG_BUF_ITERATION: src = r->iteration; need = sizeof(cvg_u32); break;
     case CVG_BUF_STATS: src = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
     case CVG_BUF_SCALE_EXP: src = r->scale_exp; need = sizeof(int); break;
+    case CVG_BUF_BIN_EXP: src = r->bin_exp; need = sizeof(int) * ((size_t)D * N + 1); break;
     default: return fail(CVG_ERR_INVALID, "unknown buffer");
     }
     if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
@@ -1073,8 +1108,23 @@ cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out)
         cudaFree(x);
         cudaFree(y);
         *out = 2.0 * bytes / (best * 1e-3) / 1e9;
+    } else if (kind >= 3 && kind <= 6) {
+        double *sink = nullptr;
+        CK(cudaMalloc(&sink, sizeof(double)));
+        const int blocks = ctx->n_sm * 2, iters = 4096;
+        for (int rep = 0; rep < 4; ++rep) {
+            CK(cudaEventRecord(a, s));
+            CK(cvg_launch_smem_atomic_bench(kind - 3, blocks, iters, sink, s));
+            CK(cudaEventRecord(b, s));
+            CK(cudaEventSynchronize(b));
+            float t;
+            CK(cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) best = std::min(best, t);
+        }
+        cudaFree(sink);
+        *out = (double)blocks * 512.0 * iters / (best * 1e-3) / 1e9;   // G atomics/s
     } else {
-        return fail(CVG_ERR_INVALID, "kind must be 0, 1 or 2");
+        return fail(CVG_ERR_INVALID, "kind must be in [0, 6]");
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);

@@ -42,6 +42,10 @@ cvg_status cvg_internal_compile_only(const std::string &src, const char *arch, s
 const char *cvg_internal_src_common();
 const char *cvg_internal_src_fill();
 double cvg_internal_now_ms();
+// FP32-form scale exponent k from the pilot: 2^k near the rms of f*jac
+// (sum of squares ss over n samples), raised so that the largest seen
+// |f*jac| (binary exponent emax) stays below 2^60 after scaling.
+int cvg_internal_pilot_scale(int emax, double ss, double n);
 // Weighted mean, error, chi^2/dof from per-iteration stats [3][max_it].
 void cvg_internal_result(const double *stats, int max_it, int done, int skip, cvg_result *out);
 

@@ -11,6 +11,7 @@
 // 667-694) and the histogram reset (src/main.cu:147-158).
 #include "cvg_kernels.cuh"
 
+#include <climits>
 #include <cooperative_groups.h>
 namespace cg = cooperative_groups;
 
@@ -469,6 +470,21 @@ __global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb) 
 constexpr int CL = 8;      // CTAs per cluster (portable size)
 constexpr int KB = 128;    // threads per CTA
 
+// Dynamic shared memory of one K4 CTA: doubles w[B+2] sw[B] cs[B] fsw[N]
+// fcs[N] xo[N+1] fw[N], then ints fdv[N] eb[B].
+__host__ __device__ inline size_t k4_smem_bytes(int N)
+{
+    const size_t B = (size_t)((N + CL - 1) / CL);
+    return sizeof(double) * (3 * B + 4 * (size_t)N + 3) + sizeof(int) * ((size_t)N + B) + 16;
+}
+
+// Binary exponent of a positive finite double (denormals: -1023), else INT_MIN.
+__device__ __forceinline__ int k4_exponent(double v)
+{
+    if (!(v > 0.0) || !isfinite(v)) return INT_MIN;
+    return (int)((__double_as_longlong(v) >> 52) & 0x7FF) - 1023;
+}
+
 __device__ __forceinline__ double cl_sum(cg::cluster_group &cl, double *slot)
 {
     double t = 0.0;
@@ -481,14 +497,20 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
     extern __shared__ __align__(16) double ks[];
     __shared__ double part[4];
     __shared__ double wscr[KB / 32];
+    __shared__ int iscr[KB / 32];
+    __shared__ int emin_slot;
     cg::cluster_group cl = cg::this_cluster();
     const int r = (int)cl.block_rank();
     const int N = a.n_intervals, tid = threadIdx.x;
     const int B = (N + CL - 1) / CL;
     const int i0 = min(N, r * B), i1 = min(N, i0 + B), nb = i1 - i0;
-    // smem: w[B+2] (with halo) | sw[B] | cs[B] | fsw[N] | fcs[N] | xo[N+1] | fdv[N] (int)
+    // smem: w[B+2] (with halo) | sw[B] | cs[B] | fsw[N] | fcs[N] | xo[N+1] | fw[N] | fdv[N] | eb[B]
     double *w = ks, *sw = w + B + 2, *cs = sw + B, *fsw = cs + B, *fcs = fsw + N, *xo = fcs + N;
-    int *fdv = (int *)(xo + N + 1);
+    double *fw = xo + N + 1;
+    int *fdv = (int *)(fw + N), *eb = fdv + N;
+    // FP32 form: per-bin exponents of the expected per-sample (f*jac)^2 of the
+    // next fill (see the fill's histogram update); eb holds this CTA's bins
+    const bool ex = a.bin_exp != nullptr;
     double *xe = a.x_edges + (size_t)d * (N + 1);
     float *xe32 = a.x_edges32 + (size_t)d * (N + 1);
 
@@ -574,7 +596,12 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
             for (int q = 0; q < CL; ++q) {
                 const int q0 = min(N, q * B), q1 = min(N, q0 + B);
                 const double *rsw = cl.map_shared_rank(sw, q), *rcs = cl.map_shared_rank(cs, q);
-                for (int j = tid; j < q1 - q0; j += KB) { fsw[q0 + j] = rsw[j]; fcs[q0 + j] = rcs[j]; }
+                const double *rw = cl.map_shared_rank(w, q);
+                for (int j = tid; j < q1 - q0; j += KB) {
+                    fsw[q0 + j] = rsw[j];
+                    fcs[q0 + j] = rcs[j];
+                    if (ex) fw[q0 + j] = rw[j + 1];
+                }
             }
             __syncthreads();
             const double delta = ssum / N;
@@ -593,13 +620,52 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
                 const double xn = fma(acc / fsw[o], xo[o + 1] - xo[o], xo[o]);
                 xe[k + 1] = xn;
                 xe32[k + 1] = (float)xn;
+                // new bin k ends in old bin o, where it is delta/fsw[o] of o's
+                // width wide: its samples' (f*jac)^2 scale by that ratio squared
+                if (ex) {
+                    const double rr = fsw[o] > 0.0 ? delta / fsw[o] : 1.0;
+                    eb[k - i0] = k4_exponent(fw[o] * rr * rr);
+                }
+            }
+            if (ex && i1 == N && i0 < N && tid == 0) {
+                const double rr = fsw[N - 1] > 0.0 ? delta / fsw[N - 1] : 1.0;
+                eb[N - 1 - i0] = k4_exponent(fw[N - 1] * rr * rr);
             }
             if (r == 0 && tid == 0) xe32[0] = (float)xo[0];
             if (i1 == N && i0 < N && tid == 0) xe32[N] = (float)xo[N];
         }
     }
-    if (!ok && nb > 0)
+    if (!ok && nb > 0) {
         for (int i = i0 + tid; i <= (i1 == N ? N : i1 - 1); i += KB) xe32[i] = (float)xo[i];
+        if (ex)
+            for (int i = i0 + tid; i < i1; i += KB) eb[i - i0] = k4_exponent(w[i - i0 + 1]);
+    }
+    if (ex) {
+        // bins without an estimate (no samples, zero weight) take the
+        // dimension's smallest exponent; stored unscaled (+2k of the fill)
+        __syncthreads();
+        int mn = INT_MAX;
+        for (int i = tid; i < nb; i += KB)
+            if (eb[i] != INT_MIN) mn = min(mn, eb[i]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+        if ((tid & 31) == 0) iscr[tid >> 5] = mn;
+        __syncthreads();
+        if (tid == 0) {
+            int m = INT_MAX;
+            for (int q = 0; q < KB / 32; ++q) m = min(m, iscr[q]);
+            emin_slot = m;
+        }
+        cl.sync();
+        int cmn = INT_MAX;
+        for (int q = 0; q < CL; ++q) cmn = min(cmn, *cl.map_shared_rank(&emin_slot, q));
+        if (cmn == INT_MAX) cmn = 0;
+        const int kused = a.bin_exp[a.dim * N];
+        for (int i = tid; i < nb; i += KB) {
+            const int e = eb[i] != INT_MIN ? eb[i] : cmn;
+            a.bin_exp[(size_t)d * N + i0 + i] = e + 2 * kused;
+        }
+    }
     cl.sync();   // keep shared memory alive until every CTA has read it
 }
 
@@ -659,7 +725,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine_b(cvg
 {
     const unsigned cid = blockIdx.x / CL;
     const int i = find_inst(B.dim_base, B.n, cid);
-    k4_refine_dev(B.R[i], (int)(cid - B.dim_base[i]));
+    if (B.keep_grid) {
+        cvg_refine_args a = B.R[i];
+        a.adapt = 0;
+        k4_refine_dev(a, (int)(cid - B.dim_base[i]));
+    } else {
+        k4_refine_dev(B.R[i], (int)(cid - B.dim_base[i]));
+    }
 }
 
 // Global tile numbering of the next batched fill: tile_base[i] = first tile
@@ -723,6 +795,23 @@ __global__ void __launch_bounds__(256) fma_bench(int iters, double *sink)
     if (s == (T)-1.2345) sink[0] = (double)s;
 }
 
+// Shared-memory atomic throughput: every thread adds to random words of a
+// 4096-word table (the access pattern of the fill's bin histograms).
+template <typename V>
+__global__ void __launch_bounds__(512) smem_atomic_bench(int iters, double *sink)
+{
+    __shared__ V tab[4096];
+    for (int i = threadIdx.x; i < 4096; i += blockDim.x) tab[i] = (V)0;
+    __syncthreads();
+    cvg_u32 x = threadIdx.x * 2654435761u + blockIdx.x * 40503u + 1u;
+    for (int k = 0; k < iters; ++k) {
+        x ^= x << 13; x ^= x >> 17; x ^= x << 5;
+        atomicAdd(&tab[x & 4095u], (V)1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && (double)tab[7] == -1.0) sink[0] = 1.0;
+}
+
 __global__ void copy_bench(const float4 *__restrict__ src, float4 *__restrict__ dst, size_t n)
 {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -736,6 +825,16 @@ cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, 
 {
     if (kind == 0) fma_bench<float><<<blocks, 256, 0, s>>>(iters, sink);
     else fma_bench<double><<<blocks, 256, 0, s>>>(iters, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_smem_atomic_bench(int kind, int blocks, int iters, double *sink,
+                                         cudaStream_t s)
+{
+    if (kind == 0) smem_atomic_bench<float><<<blocks, 512, 0, s>>>(iters, sink);
+    else if (kind == 1) smem_atomic_bench<cvg_u32><<<blocks, 512, 0, s>>>(iters, sink);
+    else if (kind == 2) smem_atomic_bench<cvg_u64><<<blocks, 512, 0, s>>>(iters, sink);
+    else smem_atomic_bench<double><<<blocks, 512, 0, s>>>(iters, sink);
     return cudaGetLastError();
 }
 
@@ -772,9 +871,7 @@ cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cuda
 
 cudaError_t cvg_launch_refine(const cvg_refine_args &a, cudaStream_t s)
 {
-    const int N = a.n_intervals, B = (N + CL - 1) / CL;
-    const size_t smem = sizeof(double) * ((size_t)(B + 2) + 2 * B + 2 * (size_t)N + N + 1) +
-                        sizeof(int) * (size_t)N + 16;
+    const size_t smem = k4_smem_bytes(a.n_intervals);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k4_refine, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
@@ -822,9 +919,7 @@ cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_ba
 
 cudaError_t cvg_launch_refine_batch(const cvg_refine_batch &B, int n_intervals, cudaStream_t s)
 {
-    const int N = n_intervals, Bk = (N + CL - 1) / CL;
-    const size_t smem = sizeof(double) * ((size_t)(Bk + 2) + 2 * Bk + 2 * (size_t)N + N + 1) +
-                        sizeof(int) * (size_t)N + 16;
+    const size_t smem = k4_smem_bytes(n_intervals);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k4_refine_b, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

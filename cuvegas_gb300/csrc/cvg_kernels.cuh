@@ -55,6 +55,8 @@ struct cvg_refine_args {
     float *x_edges32;       // [dim][N+1]
     double *weights;        // [dim][N], read then zeroed
     cvg_u32 *counts;        // [dim][N], read then zeroed
+    int *bin_exp;           // FP32 form: [dim][N+...] per-bin exponents for the next fill
+                            // (written), [dim*N] = scale exponent of the fill (read); or null
     double alpha;
     int dim;
     int n_intervals;
@@ -75,6 +77,7 @@ struct cvg_refine_batch {
     const unsigned *dim_base;     // [n+1] prefix of dimensions
     unsigned total_dims;
     int n;
+    int keep_grid;                // 1: every instance as with adapt = 0
 };
 
 __host__ __device__ inline unsigned cvg_realloc_blocks(cvg_u32 n_cubes)
@@ -93,6 +96,8 @@ cudaError_t cvg_launch_grid32(const double *x, float *x32, int n, cudaStream_t s
 // Peak-throughput microbenchmarks (FP32 / FP64 FMA chains, device copy).
 cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, cudaStream_t s);
 cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cudaStream_t s);
+cudaError_t cvg_launch_smem_atomic_bench(int kind, int blocks, int iters, double *sink,
+                                         cudaStream_t s);
 // Fill n words with a value.
 cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
 

@@ -152,9 +152,13 @@ enum {
                                 the next fills instead of Philox (parity tests); 0 bytes
                                 switches back                                         */
     CVG_BUF_STATS = 11,      /* double [3][max_it]       get: I_it, sigma2_it, samples_it */
-    CVG_BUF_SCALE_EXP = 12   /* int32  [1]               get/set: FP32 form carries f*jac
+    CVG_BUF_SCALE_EXP = 12,  /* int32  [1]               get/set: FP32 form carries f*jac
                                 scaled by 2^-k (k chosen by a pilot, then updated each
                                 iteration) so (f*jac)^2 stays in float range             */
+    CVG_BUF_BIN_EXP = 13     /* int32  [dim*N+1]         get: FP32 form, binary exponent of
+                                each bin's expected per-sample (f*jac)^2 for the next fill
+                                (unscaled; set by the pilot, then by each refinement); the
+                                last entry is the k of the last fill                      */
 };
 cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
 cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);
@@ -253,7 +257,9 @@ cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_sum, uint32
                                int32_t tile_samples, void *stream);
 
 /* Throughput microbenchmark of this device: kind 0 = FP32 FMA, 1 = FP64 FMA
- * (TFLOP/s, 2 flops per FMA), 2 = device-memory copy (GB/s, read+write). */
+ * (TFLOP/s, 2 flops per FMA), 2 = device-memory copy (GB/s, read+write),
+ * 3..6 = shared-memory atomic adds to random words of a 4096-word table,
+ * float / u32 / u64 / double (G atomics/s). */
 cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out);
 
 #ifdef __cplusplus

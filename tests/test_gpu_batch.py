@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from cuvegas_gb300 import _lib as L, autotune, batch as B, integrands as I, runtime
-from oracle import analytic as A
+from cuvegas_gb300 import analytic as A
 
 pytestmark = pytest.mark.gpu
 PPD = [2 * d for d in range(17)]

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from cuvegas_gb300 import _lib as L, integrands as I, runtime
-from oracle import analytic as A
+from cuvegas_gb300 import analytic as A
 
 pytestmark = pytest.mark.gpu
 

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from cuvegas_gb300 import _lib as L, integrands as I, runtime
-from oracle import analytic as A
+from cuvegas_gb300 import analytic as A
 from oracle import pyoracle as P
 
 pytestmark = pytest.mark.gpu
@@ -46,6 +46,70 @@ def test_fill_fp64_matches_oracle(ctx, dim, n_it, N):
     np.testing.assert_allclose(JF, o.JF, rtol=1e-12, atol=1e-300)
     np.testing.assert_allclose(JF2, o.JF2, rtol=1e-12, atol=1e-300)
     np.testing.assert_allclose(W, o.weights, rtol=1e-11, atol=1e-300)
+
+
+def test_fill_fp32_histograms_against_oracle(ctx):
+    """FP32 form: per-bin sums of (f*jac)^2 (fixed point in shared memory,
+    wraps and large weights in FP64) against the FP64 oracle on the same
+    Philox words.  The FP32 map may put a sample in the neighbouring bin when
+    y*N lies within FP32 rounding of an integer."""
+    dim, n_it, N = 3, 200000, 64
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=5, prec=L.PREC_FP32) as r:
+        k = int(r.get(L.BUF_SCALE_EXP)[0])
+        r.step(L.STAGE_FILL)
+        JF, W, Cn = r.get(L.BUF_JF), r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+    W = W * 4.0 ** k
+    o = oracle_run(dim, n_it, 4, N)
+    u, _ = P.uniforms(P.U_PHILOX_F32, seed=5)
+    S = o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    assert Cn.sum() == S * dim
+    assert np.abs(Cn.astype(np.int64) - o.counts).sum() <= 2e-4 * S * dim
+    np.testing.assert_allclose(W.sum(axis=1), o.weights.sum(axis=1), rtol=2e-5)
+    # every bin to its own relative precision, also the tail bins whose sums
+    # are ~1e-20 of the central ones (the refinement's damping weighs them)
+    assert o.weights.min() < 1e-15 * o.weights.max()
+    np.testing.assert_allclose(W, o.weights, rtol=2e-3, atol=0)
+    np.testing.assert_allclose(JF.sum(), o.JF.sum(), rtol=1e-5)
+
+
+def test_fp32_bin_exponent_table(ctx):
+    """The pilot's table of per-bin weight exponents follows the integrand:
+    central bins of the Gaussian far above the tails; each refinement
+    replaces it with one for the new bins."""
+    dim, n_it, N = 3, 200000, 64
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=5, prec=L.PREC_FP32) as r:
+        t0 = r.get(L.BUF_BIN_EXP)
+        r.iterate(2)
+        t1 = r.get(L.BUF_BIN_EXP)
+        k = int(r.get(L.BUF_SCALE_EXP)[0])
+    e0 = t0[:-1].reshape(dim, N)
+    assert t0[-1] == 0                                   # pilot sums are unscaled
+    assert np.all(e0[:, N // 2] > e0[:, 0] + 40)         # exp(-2*25) ~ 2^-72 at the edge
+    assert np.all(np.abs(e0[:, N // 2] - e0[:, N // 2 - 1]) < 4)
+    e1 = t1[:-1].reshape(dim, N)
+    assert not np.array_equal(e0, e1)
+    # after adaptation the bins are far closer in expected weight
+    assert np.ptp(e1) < np.ptp(e0)
+    assert abs(int(t1[-1]) - k) <= 4
+
+
+def test_fill_fp32_histogram_word_wraps(ctx):
+    """f = 1 on the uniform grid: every sample adds weight 1 (2^16 fixed-point
+    units) to its bin.  A tile of 65536 consecutive samples (16384 cubes) lies
+    in one bin and puts 2^32 units in it, so its shared-memory word wraps; the
+    bin sums must still equal the counts exactly."""
+    n_it = 40_000_000
+    with make_run(ctx, I.CONST_ONE, 1, n_it, 2, N=2, seed=1, prec=L.PREC_FP32,
+                  block=1024, spt=64) as r:
+        assert int(r.get(L.BUF_SCALE_EXP)[0]) == 0
+        assert r.info.block * r.info.spt == 65536
+        r.step(L.STAGE_FILL)
+        W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+        r.step(L.STAGE_REALLOC | L.STAGE_REFINE)
+        res, it_res, _ = r.result()
+    assert Cn.sum() == n_it
+    assert np.array_equal(W, Cn.astype(np.float64))
+    assert it_res[0] == 1.0
 
 
 def test_fill_replay_uniforms_matches_oracle(ctx):

@@ -5,7 +5,7 @@ import math
 import numpy as np
 import pytest
 
-from oracle import analytic as A
+from cuvegas_gb300 import analytic as A
 from oracle import pyoracle as P
 
 # Published Philox4x32-10 known-answer vectors (Random123 kat_vectors).
