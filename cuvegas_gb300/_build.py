@@ -1,8 +1,9 @@
-"""Build libcuvegas.so in-tree for sm_103a.
+"""Build libcuvegas.so in-tree for sm_103a, and the cuvegas command-line driver.
 
 Steps: embed the device headers (for NVRTC) into a generated include, compile
-the two translation units with nvcc in parallel, link one shared library with
-the CUDA runtime linked statically and NVRTC dynamically.
+the translation units with nvcc in parallel, link one shared library with
+the CUDA runtime linked statically and NVRTC dynamically, then compile the
+host-only CLI (cli/cuvegas_cli.cpp) against it.
 """
 import concurrent.futures as cf
 import os
@@ -15,6 +16,8 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libcuvegas.so")
+CLI = os.path.join(LIBDIR, "cuvegas")
+CLI_SRC = os.path.join(PKG, "cli", "cuvegas_cli.cpp")
 INCLUDE = os.path.join(ROOT, "include")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EMBED = ["cvg_common.cuh", "cvg_fill.cuh"]
@@ -49,6 +52,7 @@ def _embed(out_path):
 def _inputs():
     files = [os.path.join(CSRC, n) for n in os.listdir(CSRC)]
     files.append(os.path.join(INCLUDE, "cuvegas.h"))
+    files.append(CLI_SRC)
     files.append(os.path.abspath(__file__))
     return files
 
@@ -59,7 +63,8 @@ def build(force=False, verbose=False):
     gen = os.path.join(BUILD, "cvg_embedded.inc")
     _embed(gen)
     newest = max(os.path.getmtime(p) for p in _inputs())
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest
+            and os.path.exists(CLI) and os.path.getmtime(CLI) >= newest):
         return LIB
     nvcc = os.path.join(cuda_home(), "bin", "nvcc")
     if not os.path.exists(nvcc):
@@ -87,7 +92,22 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    _build_cli(verbose)
     return LIB
+
+
+def _build_cli(verbose=False):
+    """Host-only C++ driver; finds libcuvegas.so next to itself."""
+    cxx = shutil.which("g++") or shutil.which("c++") or "g++"
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, CLI_SRC, "-o", tmp, "-L", LIBDIR,
+           "-lcuvegas", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd))
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, CLI)
 
 
 if __name__ == "__main__":
