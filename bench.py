@@ -35,10 +35,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 DIM, N_IT, NBINS, ITERS, SEED = 8, 100_000_000, 1024, 20, 0
-FLOPS_PER_EVAL = 11 * DIM + 4          # algorithmic FP32 ops per evaluation
+def _hbm_gbs():
+    """Measured copy bandwidth of the GB300s (MEASURED_PEAKS.json)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0                      # fallback figure of one earlier GB300 measurement
+
+
+HBM_GBS = _hbm_gbs()
+FLOPS_PER_EVAL = 11 * DIM + 4          # algorithmic FP32 ops per evaluation (map 7/dim, integrand 4/dim, 4)
+SFU_PER_EVAL = DIM                     # one exp per dimension
+PHILOX_PER_EVAL = (DIM + 3) // 4       # Philox4x32-10 calls per evaluation (4 uniforms per call)
 METRIC = "integrand evals/s, VEGAS+ Gaussian d=8, 1e8 evals/iteration (FP32-compensated form)"
 WORKLOAD = "gauss-d8-1e8x20-fp32kahan"
-LAUNCHES_PER_IT = 7                    # fill + refine + 5 reallocation kernels
+LAUNCHES_PER_IT = 5                    # fill, 3 reallocation kernels (finish and scan are their tails), refinement
 
 
 def _dist():
@@ -105,12 +117,37 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def fill_roofline(ctx, evals_per_launch, mean_ms, fp_eval, sfu_eval, philox_eval):
+    """Compute roofline of a fill launch: evaluations/s are bounded by each
+    pipe alone -- FP32 ops, special-function (exp) ops, Philox calls of the
+    sampler -- with peaks measured live on this GPU (cvg_measure_peak).  The
+    binding pipe is reported; frac = measured evals/s / that pipe's bound."""
+    p_fp32 = ctx.measure_peak(0) / 2.0         # T FP32 instructions/s (FMA = 2 flops)
+    p_sfu = ctx.measure_peak(8)                # T ex2/s
+    p_philox = ctx.measure_peak(9)             # T Philox calls/s
+    rate = evals_per_launch / (mean_ms * 1e-3)
+    ceil = {"fp32": (p_fp32 * 1e12 / fp_eval, fp_eval, p_fp32, "T FP32 ops/s"),
+            "sfu": (p_sfu * 1e12 / max(sfu_eval, 1e-9), sfu_eval, p_sfu, "T ex2/s"),
+            "sampler": (p_philox * 1e12 / philox_eval, philox_eval, p_philox, "T Philox calls/s")}
+    bound = min(ceil, key=lambda k: ceil[k][0])
+    evals_max, per_eval, peak, unit = ceil[bound]
+    achieved = rate * per_eval / 1e12
+    return {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "traffic": None,
+            "ceilings_evals_per_s": {k: v[0] for k, v in ceil.items()},
+            "evals_per_s_fill": rate, "fill_ms_mean": mean_ms,
+            "evals_per_launch": evals_per_launch,
+            "per_eval": {"fp32_ops": fp_eval, "ex2": sfu_eval, "philox_calls": philox_eval},
+            "peak_source": "live microbenchmarks of this GPU (cvg_measure_peak kinds 0, 8, 9); "
+                           "MEASURED_PEAKS.json holds HBM and bf16 figures only"}
+
+
 def _ncu_traffic():
-    """DRAM bytes per fill launch from the committed ncu summary (or None)."""
+    """DRAM bytes per evaluation of the fill from the committed ncu summary (or None)."""
     p = os.path.join(ROOT, "profiles", "fill_gauss_d8_traffic.txt")
     try:
         for line in open(p):
-            if line.startswith("dram_bytes_per_launch_full_size="):
+            if line.startswith("dram_bytes_per_eval="):
                 return float(line.split("=", 1)[1])
     except OSError:
         pass
@@ -297,16 +334,17 @@ def run_ours(args):
     if rank == 0 and len(fills):
         mean_ms = float(np.mean(fills))
         evals_per_launch = float(np.mean(chosen["samples"]))
-        achieved = evals_per_launch * FLOPS_PER_EVAL / (mean_ms * 1e-3) / 1e12
-        peak = ctx.measure_peak(0)
-        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": _ncu_traffic(),
-                "kernel": "cvg_fill_entry (FP32, d=8, 1024 bins)",
-                "fill_ms_mean": mean_ms, "evals_per_launch": evals_per_launch,
-                "flops_per_eval": FLOPS_PER_EVAL,
-                "peak_source": "FP32 FMA microbenchmark of this GPU (cvg_measure_peak), "
-                               "live; MEASURED_PEAKS.json holds no FP32 figure",
-                "fill_share_of_step": mean_ms / (chosen["ms"] / steps)}
+        roof = fill_roofline(ctx, evals_per_launch, mean_ms, FLOPS_PER_EVAL, SFU_PER_EVAL,
+                             PHILOX_PER_EVAL)
+        roof["kernel"] = "cvg_fill_entry (FP32, d=8, 1024 bins)"
+        roof["fill_share_of_step"] = mean_ms / (chosen["ms"] / steps)
+        tr = _ncu_traffic()
+        if tr:
+            roof["traffic"] = tr * evals_per_launch   # ncu DRAM bytes per evaluation x evaluations
+            roof["traffic_note"] = ("ncu dram__bytes_read+write of the fill at 3e7 evals, per "
+                                    "evaluation, scaled to this launch; HBM share %.1f%% of %.0f GB/s"
+                                    % (100 * roof["traffic"] / (mean_ms * 1e-3) / 1e9 / HBM_GBS,
+                                       HBM_GBS))
 
     # end to end through the C ABI: host params in, host result out
     e2e = None

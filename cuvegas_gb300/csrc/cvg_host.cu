@@ -1123,8 +1123,41 @@ cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out)
         }
         cudaFree(sink);
         *out = (double)blocks * 512.0 * iters / (best * 1e-3) / 1e9;   // G atomics/s
+    } else if (kind == 10 || kind == 11) {
+        double *gw = nullptr;
+        CK(cudaMalloc(&gw, 4096 * sizeof(double)));
+        CK(cudaMemsetAsync(gw, 0, 4096 * sizeof(double), s));
+        const int blocks = ctx->n_sm * 4, iters = 4096;
+        for (int rep = 0; rep < 5; ++rep) {
+            CK(cudaEventRecord(a, s));
+            CK(cvg_launch_hist_update_bench(kind - 10, blocks, iters, gw, s));
+            CK(cudaEventRecord(b, s));
+            CK(cudaEventSynchronize(b));
+            float t;
+            CK(cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) best = std::min(best, t);
+        }
+        cudaFree(gw);
+        *out = (double)blocks * 512.0 * iters / (best * 1e-3) / 1e9;   // G updates/s
+    } else if (kind >= 7 && kind <= 9) {
+        double *sink = nullptr;
+        CK(cudaMalloc(&sink, sizeof(double)));
+        const int blocks = ctx->n_sm * 8;
+        const int iters = kind == 9 ? 256 : 2048;
+        for (int rep = 0; rep < 4; ++rep) {
+            CK(cudaEventRecord(a, s));
+            CK(cvg_launch_pipe_bench(kind - 7, blocks, iters, sink, s));
+            CK(cudaEventRecord(b, s));
+            CK(cudaEventSynchronize(b));
+            float t;
+            CK(cudaEventElapsedTime(&t, a, b));
+            if (rep > 0) best = std::min(best, t);
+        }
+        cudaFree(sink);
+        const double per_iter = kind == 9 ? 4.0 : 8.0;   // Philox calls / ops per iteration
+        *out = per_iter * iters * 256.0 * blocks / (best * 1e-3) / 1e12;   // T ops (calls)/s
     } else {
-        return fail(CVG_ERR_INVALID, "kind must be in [0, 6]");
+        return fail(CVG_ERR_INVALID, "kind must be in [0, 11]");
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);

@@ -795,6 +795,58 @@ __global__ void __launch_bounds__(256) fma_bench(int iters, double *sink)
     if (s == (T)-1.2345) sink[0] = (double)s;
 }
 
+// Pipe throughput microbenchmarks for the fill's roofline (8 independent
+// chains per thread, 256 threads, 8 CTAs per SM).
+// INT32 multiply-add (the sampler's and the bin arithmetic's integer work).
+__global__ void __launch_bounds__(256) int_bench(int iters, double *sink)
+{
+    cvg_u32 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = threadIdx.x * 7u + (cvg_u32)i;
+    const cvg_u32 m = 0x9E3779B1u, c = blockIdx.x | 1u;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = a[i] * m + c;
+    }
+    cvg_u32 s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s ^= a[i];
+    if (s == 0x12345678u) sink[0] = (double)s;
+}
+// Special-function unit: ex2.approx (the integrands' exp).
+__global__ void __launch_bounds__(256) sfu_bench(int iters, double *sink)
+{
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = 0.001f * (float)(threadIdx.x + i);
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            float r;
+            asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a[i]));
+            a[i] = r - 1.0f;
+        }
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i];
+    if (s == -1.2345f) sink[0] = (double)s;
+}
+// Philox4x32-10 calls (the sampler: one call per 4 dimensions of a sample).
+__global__ void __launch_bounds__(256) philox_bench(int iters, double *sink)
+{
+    cvg_u32 acc = 0;
+    const cvg_u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const cvg_u32x4 r = cvg_philox((cvg_u32)k, t, (cvg_u32)i, 7u, 0x1234u, 0x5678u);
+            acc ^= r.x ^ r.y ^ r.z ^ r.w;
+        }
+    }
+    if (acc == 0x12345678u) sink[0] = (double)acc;
+}
+
 // Shared-memory atomic throughput: every thread adds to random words of a
 // 4096-word table (the access pattern of the fill's bin histograms).
 template <typename V>
@@ -825,6 +877,51 @@ cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, 
 {
     if (kind == 0) fma_bench<float><<<blocks, 256, 0, s>>>(iters, sink);
     else fma_bench<double><<<blocks, 256, 0, s>>>(iters, sink);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_pipe_bench(int kind, int blocks, int iters, double *sink, cudaStream_t s)
+{
+    if (kind == 0) int_bench<<<blocks, 256, 0, s>>>(iters, sink);
+    else if (kind == 1) sfu_bench<<<blocks, 256, 0, s>>>(iters, sink);
+    else philox_bench<<<blocks, 256, 0, s>>>(iters, sink);
+    return cudaGetLastError();
+}
+
+// The fill's per-(dimension, bin) histogram update in its two forms: MODE 0
+// = float atomicAdd of the weight + u32 count; MODE 1 = u32 fixed-point add
+// whose wrap carries into a global FP64 word + u32 count.  Lanes of a warp
+// draw bins from a 128-bin window, as samples of one stratum do.
+template <int MODE>
+__global__ void __launch_bounds__(512) hist_update_bench(int iters, double *gw)
+{
+    __shared__ cvg_u32 lo[4096];
+    __shared__ cvg_u32 cn[4096];
+    for (int i = threadIdx.x; i < 4096; i += blockDim.x) { lo[i] = 0u; cn[i] = 0u; }
+    __syncthreads();
+    cvg_u32 x = threadIdx.x * 2654435761u + blockIdx.x * 40503u + 1u;
+    const cvg_u32 base = ((threadIdx.x >> 5) * 128u) & 4095u;
+    for (int it = 0; it < iters; ++it) {
+        x ^= x << 13; x ^= x >> 17; x ^= x << 5;
+        const cvg_u32 i = (base + (x & 127u) + (cvg_u32)it * 512u) & 4095u;
+        const float w = __uint_as_float(0x3F800000u | (x >> 9)) - 0.5f;   // [0.5, 1.5)
+        if (MODE == 0) {
+            atomicAdd(reinterpret_cast<float *>(&lo[i]), w);
+        } else {
+            const cvg_u32 q = __float_as_uint(__fadd_rn(w * 65536.f, 8388608.f)) - 0x4B000000u;
+            const cvg_u32 o = atomicAdd(&lo[i], q);
+            if (o + q < o) atomicAdd(&gw[i], 65536.0);
+        }
+        atomicAdd(&cn[i], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && lo[5] == 0xFFFFFFFFu && cn[3] == 7u) gw[0] = -1.0;
+}
+
+cudaError_t cvg_launch_hist_update_bench(int mode, int blocks, int iters, double *gw, cudaStream_t s)
+{
+    if (mode == 0) hist_update_bench<0><<<blocks, 512, 0, s>>>(iters, gw);
+    else hist_update_bench<1><<<blocks, 512, 0, s>>>(iters, gw);
     return cudaGetLastError();
 }
 

@@ -98,6 +98,10 @@ cudaError_t cvg_launch_fma_bench(int kind, int blocks, int iters, double *sink, 
 cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cudaStream_t s);
 cudaError_t cvg_launch_smem_atomic_bench(int kind, int blocks, int iters, double *sink,
                                          cudaStream_t s);
+// mode 0: float atomic + count, 1: u32 fixed point with carry + count (gw: 4096 doubles)
+cudaError_t cvg_launch_hist_update_bench(int mode, int blocks, int iters, double *gw, cudaStream_t s);
+// kind 0: INT32 multiply-add, 1: ex2.approx, 2: Philox4x32-10 (4 calls per iteration)
+cudaError_t cvg_launch_pipe_bench(int kind, int blocks, int iters, double *sink, cudaStream_t s);
 // Fill n words with a value.
 cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
 

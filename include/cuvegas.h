@@ -259,7 +259,10 @@ cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_sum, uint32
 /* Throughput microbenchmark of this device: kind 0 = FP32 FMA, 1 = FP64 FMA
  * (TFLOP/s, 2 flops per FMA), 2 = device-memory copy (GB/s, read+write),
  * 3..6 = shared-memory atomic adds to random words of a 4096-word table,
- * float / u32 / u64 / double (G atomics/s). */
+ * float / u32 / u64 / double (G atomics/s), 7 = INT32 multiply-add (T ops/s),
+ * 8 = ex2.approx (T ops/s), 9 = Philox4x32-10 (T calls/s), 10/11 = the fill's
+ * per-bin histogram update with a float atomic / with the u32 fixed-point
+ * atomic, each with its count atomic (G updates/s). */
 cvg_status cvg_measure_peak(cvg_context ctx, int32_t kind, double *out);
 
 #ifdef __cplusplus

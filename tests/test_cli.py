@@ -66,6 +66,8 @@ def test_cli_run_prints_reference_lines():
     out = dict(pairs)
     exact = math.erf(5.0) ** 4
     res, err = float(out["Result"]), float(out["Error"])
-    assert int(out["Total evals"]) <= 4000000 and int(out["Total evals"]) > 3_900_000
-    assert int(out["Strat"]) == int((400000 / 4) ** 0.25)
+    n_strat, n_cubes = int(out["Strat"]), int(out["Cubes"])
+    assert n_strat == int((400000 / 4) ** 0.25) and n_cubes == n_strat ** 4
+    # n_h >= 2 per cube: an iteration takes up to N_it + 2 n_cubes samples
+    assert 0.8 * 4000000 < int(out["Total evals"]) <= 10 * (400000 + 2 * n_cubes)
     assert abs(res - exact) < 5 * err
