@@ -87,7 +87,7 @@ def build(force=False, verbose=False):
     libdir = os.path.join(cuda_home(), "lib64")
     tmp = LIB + ".tmp%d" % os.getpid()
     cmd = [nvcc] + GENCODE + ["-shared", "-o", tmp] + objs + [
-        "-L", libdir, "-lnvrtc", "-Xlinker", "-rpath=" + libdir]
+        "-L", libdir, "-lnvrtc", "-lnvJitLink", "-Xlinker", "-rpath=" + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

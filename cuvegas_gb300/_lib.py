@@ -29,6 +29,7 @@ EXPORTS = (
     "cvg_run_last_fill_ms", "cvg_run_fill_times", "cvg_measure_peak", "cvg_realloc_noalloc",
     "cvg_batch_create", "cvg_batch_destroy", "cvg_batch_iterate", "cvg_batch_results",
     "cvg_batch_info_get", "cvg_batch_last_fill_ms", "cvg_batch_compile_check",
+    "cvg_context_trim", "cvg_compile_integrand_ptx",
 )
 NOALLOC_MAX_CUBES = 262144
 
@@ -91,6 +92,8 @@ def load():
         sig = {
             "cvg_context_create": [C.c_int, vp, C.POINTER(vp)],
             "cvg_context_destroy": [vp],
+            "cvg_context_trim": [vp],
+            "cvg_compile_integrand_ptx": [vp, C.c_char_p, C.c_char_p, C.c_int32, C.POINTER(vp)],
             "cvg_compile_integrand": [vp, C.c_char_p, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.POINTER(vp)],
             "cvg_integrand_release": [vp],

@@ -70,6 +70,7 @@ struct cvg_batch_s {
     std::vector<inst_host> inst;
     std::vector<int> params_per_dim;
     void *arena = nullptr;
+    size_t arena_bytes = 0;
     // device tables
     cvg_fill_args *d_fill = nullptr;
     cvg_realloc_args *d_realloc = nullptr;
@@ -142,6 +143,7 @@ std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
 {
     const char *T = b.p.precision == CVG_PREC_FP32 ? "float" : "double";
     std::string s = "#define CVG_JIT 1\n";
+    if (cvg_internal_fill_minb(b.ctx, b.block, b.fill_smem) >= 2) s += "#define CVG_FILL_LOWREG 1\n";
     s += cvg_internal_src_common();
     for (int d : dims) {
         s += "\nnamespace cvg_d" + std::to_string(d) + " {\nstatic constexpr int cvg_n_dim = " +
@@ -165,11 +167,12 @@ std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
              std::to_string(d) + "; };\n";
     char entry[512];
     std::snprintf(entry, sizeof(entry),
-                  "extern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_batch_entry("
+                  "extern \"C\" __global__ void __launch_bounds__(%d, %d) cvg_fill_batch_entry("
                   "const cvg_batch_args b) { cvg_fill_batch<%s, %d, cvg_disp, %d>(b); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_batch_entry("
                   "const cvg_batch_args b) { cvg_pilot_batch<%s, 32, cvg_disp>(b); }\n",
-                  b.block, T, b.block, b.p.n_intervals, T);
+                  b.block, cvg_internal_fill_minb(b.ctx, b.block, b.fill_smem), T, b.block,
+                  b.p.n_intervals, T);
     s += entry;
     return s;
 }
@@ -303,7 +306,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
                                                   "dimension do not fit shared memory");
     }
     cudaError_t e = cudaSetDevice(ctx->device);
-    if (e == cudaSuccess) e = cudaMalloc(&b->arena, total);
+    if (e == cudaSuccess) e = cvg_internal_arena_alloc(ctx, total, &b->arena, &b->arena_bytes);
     if (e != cudaSuccess) {
         delete b;
         return cvg_internal_fail(CVG_ERR_NOMEM, std::string("batch arena: ") + cudaGetErrorString(e));
@@ -494,7 +497,7 @@ cvg_status cvg_batch_destroy(cvg_batch b)
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
-    if (b->arena) cudaFree(b->arena);
+    if (b->arena) cvg_internal_arena_free(b->ctx, b->arena, b->arena_bytes);
     delete b;
     return CVG_OK;
 }

@@ -160,6 +160,24 @@ CVG_D void cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
         atomicAdd(gw + i, cvg_f2d(w));
     }
 }
+// Fixed-point update of bin i without branches: returns 1 if w did not fit
+// (the caller adds it to the global FP64 sum), 2 if the word wrapped (the
+// caller adds 2^(16+e)), 0 otherwise (almost always).
+CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
+{
+    const cvg_u32 old = atomicAdd(hc + i, 1u);
+    const int e = (int)old >> 24;
+    const float s = w * __int_as_float((143 - e) << 23);      // w * 2^(16-e)
+    const bool fits = s < 8388608.0f;
+    const cvg_u32 q = fits ? __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u : 0u;
+    const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
+    return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
+}
+CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, float w)
+{
+    if (rare & 1u) atomicAdd(gw + i, cvg_f2d(w));
+    if (rare & 2u) atomicAdd(gw + i, __hiloint2double((1039 + ((int)hc[i] >> 24)) << 20, 0));
+}
 template <bool FIX>
 CVG_D void cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
 {
@@ -172,7 +190,10 @@ template <bool FIX>
 CVG_D double cvg_hist_value(const float *hw, const cvg_u32 *hc, int i)
 {
     if (!FIX) return cvg_f2d(hw[i]);
-    return ldexp((double)reinterpret_cast<const cvg_u32 *>(hw)[i], ((int)hc[i] >> 24) - 16);
+    // lo * 2^(e-16), exactly: (2^52 + lo) * 2^(e-68) - 2^(e-16), one FP64 add
+    const int e = ((int)hc[i] >> 24) - 16;
+    const cvg_u32 lo = reinterpret_cast<const cvg_u32 *>(hw)[i];
+    return __hiloint2double((1075 + e) << 20, (int)lo) - __hiloint2double((1075 + e) << 20, 0);
 }
 template <bool FIX>
 CVG_D double cvg_hist_value(const double *hw, const cvg_u32 *, int i) { return hw[i]; }
@@ -408,13 +429,32 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
             } else {
                 const T jf = (T)F::f(x, sm.th) * jac;
                 const T jf2 = jf * jf;
+                if constexpr (H && cvg_hist_fixed<D, T>()) {
+#ifdef CVG_FILL_LOWREG
+                    // held to 64 registers (2 CTAs per SM): branches keep the
+                    // dimensions' updates apart and fewer values live
 #pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    if (H) {
-                        cvg_hist_add<cvg_hist_fixed<D, T>()>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
-                    } else {
-                        atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
-                        atomicAdd(&a.counts[d * N + bin[d]], 1u);
+                    for (int d = 0; d < D; ++d)
+                        cvg_hist_add<true>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
+#else
+                    // fixed-point bin sums; a wrap or a large weight (rare) is
+                    // handled behind a single branch per dimension
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        const int i = d * N + bin[d];
+                        const cvg_u32 rare = cvg_hist_add_fix(sm.hw, sm.hc, i, jf2);
+                        if (rare) cvg_hist_rare(sm.hc, a.weights, i, rare, jf2);
+                    }
+#endif
+                } else {
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        if (H) {
+                            cvg_hist_add<false>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
+                        } else {
+                            atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
+                            atomicAdd(&a.counts[d * N + bin[d]], 1u);
+                        }
                     }
                 }
                 a1.add(jf);

@@ -16,6 +16,7 @@
 #include "cvg_kernels.cuh"
 
 #include <cuda_runtime.h>
+#include <nvJitLink.h>
 #include <nvrtc.h>
 
 #include <algorithm>
@@ -99,6 +100,7 @@ struct cvg_run_s {
     int it_done = 0;
     // device memory (one arena)
     void *arena = nullptr;
+    size_t arena_bytes = 0;
     double *x_edges = nullptr, *weights = nullptr, *JF = nullptr, *JF2 = nullptr, *dh = nullptr;
     double *partials = nullptr, *stats = nullptr, *theta = nullptr, *grad = nullptr;
     float *x_edges32 = nullptr, *ubuf = nullptr;
@@ -169,7 +171,7 @@ void write_file(const std::string &p, const std::vector<char> &data)
 }
 
 struct variant_key {
-    int dim, prec, block, esm, hsm, replay, n_params, grad, abi, nbins;
+    int dim, prec, block, esm, hsm, replay, n_params, grad, abi, nbins, minb;
 };
 
 // Integrand adaptor type F of the fill templates: static f (value) and df
@@ -200,6 +202,7 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     const char *T = k.prec == CVG_PREC_FP32 ? "float" : "double";
     std::string s;
     s += "#define CVG_JIT 1\n";
+    if (k.minb >= 2) s += "#define CVG_FILL_LOWREG 1\n";
     s += cvg_src_common;
     s += "\nstatic constexpr int cvg_n_dim = " + std::to_string(k.dim) + ";\n";
     s += "#line 1 \"integrand.cu\"\n";
@@ -209,11 +212,11 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     s += fn_struct("cvg_fn_user", f, k.abi, k.n_params, k.grad, "");
     char entry[1024];
     std::snprintf(entry, sizeof(entry),
-                  "\nextern \"C\" __global__ void __launch_bounds__(%d) cvg_fill_entry("
+                  "\nextern \"C\" __global__ void __launch_bounds__(%d, %d) cvg_fill_entry("
                   "const cvg_fill_args a) { cvg_fill_body<%d, %s, %d, %s, %s, %s, %d, %s, cvg_fn_user, %d>(a); }\n"
                   "extern \"C\" __global__ void __launch_bounds__(256) cvg_pilot_entry("
                   "const cvg_fill_args a) { cvg_pilot_body<%d, %s, 256, %d, cvg_fn_user>(a, blockIdx.x); }\n",
-                  k.block, k.dim, T, k.block, k.esm ? "true" : "false",
+                  k.block, k.minb > 0 ? k.minb : 1, k.dim, T, k.block, k.esm ? "true" : "false",
                   k.hsm ? "true" : "false", k.replay ? "true" : "false", k.n_params,
                   k.grad ? "true" : "false", k.nbins, k.dim, T, k.n_params);
     s += entry;
@@ -255,13 +258,46 @@ std::vector<std::string> nvrtc_options(const std::string &arch)
     return o;
 }
 
-cvg_status load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *out)
+// Link a relocatable fill cubin with the integrand's PTX into one cubin.
+cvg_status jit_link(const std::vector<char> &obj, const std::string &ptx, const std::string &arch,
+                    std::vector<char> &out)
 {
-    const std::vector<std::string> opts = nvrtc_options(ctx->arch);
+    const std::string a = "-arch=" + arch;
+    const char *opts[] = {a.c_str()};
+    nvJitLinkHandle h = nullptr;
+    if (nvJitLinkCreate(&h, 1, opts) != NVJITLINK_SUCCESS) return fail(CVG_ERR_COMPILE, "nvJitLinkCreate failed");
+    nvJitLinkResult rc = nvJitLinkAddData(h, NVJITLINK_INPUT_CUBIN, obj.data(), obj.size(), "cvg_fill");
+    if (rc == NVJITLINK_SUCCESS)
+        rc = nvJitLinkAddData(h, NVJITLINK_INPUT_PTX, ptx.c_str(), ptx.size() + 1, "integrand.ptx");
+    if (rc == NVJITLINK_SUCCESS) rc = nvJitLinkComplete(h);
+    if (rc != NVJITLINK_SUCCESS) {
+        size_t n = 0;
+        std::string log;
+        if (nvJitLinkGetErrorLogSize(h, &n) == NVJITLINK_SUCCESS && n) {
+            log.assign(n, '\0');
+            nvJitLinkGetErrorLog(h, &log[0]);
+        }
+        nvJitLinkDestroy(&h);
+        return fail(CVG_ERR_COMPILE, "linking the integrand PTX failed (" + std::to_string((int)rc) + "): " + log);
+    }
+    size_t n = 0;
+    nvJitLinkGetLinkedCubinSize(h, &n);
+    out.resize(n);
+    nvJitLinkGetLinkedCubin(h, out.data());
+    nvJitLinkDestroy(&h);
+    return CVG_OK;
+}
+
+cvg_status load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *out,
+                       const std::string &link_ptx = std::string())
+{
+    std::vector<std::string> opts = nvrtc_options(ctx->arch);
+    if (!link_ptx.empty()) opts.push_back("-rdc=true");
     int nv_major = 0, nv_minor = 0;
     nvrtcVersion(&nv_major, &nv_minor);
     std::string keystr = src;
     for (auto &o : opts) keystr += "\n" + o;
+    keystr += "\n" + link_ptx;
     keystr += "\nnvrtc " + std::to_string(nv_major) + "." + std::to_string(nv_minor);
     keystr += "\n" CVG_VERSION;
     const uint64_t key = fnv1a(keystr);
@@ -280,6 +316,11 @@ cvg_status load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *o
         if (!read_file(path, cubin)) {
             std::string log;
             CKS(nvrtc_cubin(src, opts, cubin, log));
+            if (!link_ptx.empty()) {
+                std::vector<char> linked;
+                CKS(jit_link(cubin, link_ptx, ctx->arch, linked));
+                cubin.swap(linked);
+            }
             mkdirs(dir);
             write_file(path, cubin);
         }
@@ -295,7 +336,7 @@ cvg_status jit_kernel(cvg_context ctx, const cvg_integrand_s &f, const variant_k
                       cudaKernel_t *out, cudaKernel_t *pilot = nullptr)
 {
     cudaLibrary_t lib = nullptr;
-    CKS(load_module(ctx, make_source(f, k), &lib));
+    CKS(load_module(ctx, make_source(f, k), &lib, f.link_ptx));
     CK(cudaLibraryGetKernel(out, lib, "cvg_fill_entry"));
     if (pilot) CK(cudaLibraryGetKernel(pilot, lib, "cvg_pilot_entry"));
     return CVG_OK;
@@ -306,10 +347,11 @@ cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v
     cvg_context ctx = r->ctx;
     const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
     variant_key k{r->f->dim, r->p.precision, r->block, r->esm, r->hsm, replay ? 1 : 0,
-                  r->f->n_params, grad ? 1 : 0, r->f->abi, r->p.n_intervals};
+                  r->f->n_params, grad ? 1 : 0, r->f->abi, r->p.n_intervals, 1};
     if (grad) k.hsm = 0;
     const cvg_u64 smem = cvg_fill_smem_bytes(k.dim, r->p.n_intervals, tsz, k.esm, k.hsm, k.grad,
                                              r->TS, k.n_params, k.block);
+    k.minb = cvg_internal_fill_minb(ctx, k.block, smem);
     CKS(jit_kernel(ctx, *r->f, k, &v->kernel, &v->pilot));
     const void *fn = (const void *)v->kernel;
     CK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -522,9 +564,10 @@ cvg_status check_status(cvg_run_s *r)
 // Library-internal helpers used by the batch driver (cvg_internal.h)
 // ---------------------------------------------------------------------------
 cvg_status cvg_internal_fail(cvg_status st, const std::string &msg) { return fail(st, msg); }
-cvg_status cvg_internal_load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *lib)
+cvg_status cvg_internal_load_module(cvg_context ctx, const std::string &src, cudaLibrary_t *lib,
+                                    const std::string &link_ptx)
 {
-    return load_module(ctx, src, lib);
+    return load_module(ctx, src, lib, link_ptx);
 }
 std::string cvg_internal_fn_struct(const char *name, const cvg_integrand_s &f, int abi,
                                    int n_params, int grad, const std::string &ns)
@@ -539,6 +582,58 @@ cvg_status cvg_internal_compile_only(const std::string &src, const char *arch, s
 const char *cvg_internal_src_common() { return cvg_src_common; }
 const char *cvg_internal_src_fill() { return cvg_src_fill; }
 double cvg_internal_now_ms() { return now_ms(); }
+
+cudaError_t cvg_internal_arena_alloc(cvg_context ctx, size_t bytes, void **out, size_t *got)
+{
+    {
+        std::lock_guard<std::mutex> lock(ctx->arena_mu);
+        auto it = ctx->arena_cache.lower_bound(bytes);
+        if (it != ctx->arena_cache.end() && it->first <= 2 * bytes) {
+            *out = it->second;
+            *got = it->first;
+            ctx->arena_cached -= it->first;
+            ctx->arena_cache.erase(it);
+            // a debugging aid: NaN doubles / huge integers in every byte a run
+            // forgets to initialise
+            if (ctx->arena_poison) return cudaMemsetAsync(*out, 0xFF, *got, ctx->stream);
+            return cudaSuccess;
+        }
+    }
+    cudaError_t e = cudaMalloc(out, bytes);
+    if (e == cudaErrorMemoryAllocation) {   // give the cached arenas back and retry once
+        cudaGetLastError();
+        cvg_context_trim(ctx);
+        e = cudaMalloc(out, bytes);
+    }
+    *got = e == cudaSuccess ? bytes : 0;
+    if (e == cudaSuccess && ctx->arena_poison) e = cudaMemsetAsync(*out, 0xFF, bytes, ctx->stream);
+    return e;
+}
+
+void cvg_internal_arena_free(cvg_context ctx, void *p, size_t bytes)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lock(ctx->arena_mu);
+    if (bytes > ctx->arena_cache_cap) {
+        cudaFree(p);
+        return;
+    }
+    ctx->arena_cache.emplace(bytes, p);
+    ctx->arena_cached += bytes;
+    while (ctx->arena_cached > ctx->arena_cache_cap && !ctx->arena_cache.empty()) {
+        auto big = std::prev(ctx->arena_cache.end());     // drop the largest first
+        ctx->arena_cached -= big->first;
+        cudaFree(big->second);
+        ctx->arena_cache.erase(big);
+    }
+}
+
+int cvg_internal_fill_minb(cvg_context ctx, int block, size_t smem)
+{
+    const int by_smem = ctx && ctx->smem_per_sm > 0 ? (int)(ctx->smem_per_sm / (smem + 1024)) : 1;
+    const int by_regs = 65536 / (block * 64);
+    return std::max(1, std::min(by_smem, by_regs));
+}
 
 int cvg_internal_pilot_scale(int emax, double ss, double n)
 {
@@ -557,18 +652,23 @@ void cvg_internal_result(const double *stats, int max_it, int done, int skip, cv
 {
     // weighted mean over iterations >= skip (src/main.cu:698-714), error
     // 1/sqrt(sum 1/sigma^2) (src/main.cu:792); chi^2 two-pass
+    // An iteration with zero variance (an integrand constant on every
+    // hypercube; a roundoff-negative sum counts too) is exact: the result is
+    // then the mean of the exact iterations with error 0, where the
+    // reference's 1/sigma^2 weights give inf/inf = NaN.
     const int M = max_it;
-    double sw = 0.0, swr = 0.0;
-    int used = 0;
+    double sw = 0.0, swr = 0.0, s0 = 0.0;
+    int used = 0, n0 = 0;
     for (int i = skip; i < done; ++i) {
+        if (!(stats[M + i] > 0.0)) { s0 += stats[i]; ++n0; }
         sw += 1.0 / stats[M + i];
         swr += stats[i] / stats[M + i];
         ++used;
     }
-    out->result = used ? swr / sw : 0.0;
-    out->error = used ? 1.0 / std::sqrt(sw) : 0.0;
+    out->result = n0 ? s0 / n0 : (used ? swr / sw : 0.0);
+    out->error = n0 ? 0.0 : (used ? 1.0 / std::sqrt(sw) : 0.0);
     double chi2 = 0.0;
-    for (int i = skip; i < done; ++i) {
+    for (int i = skip; i < done && !n0; ++i) {
         const double dlt = stats[i] - out->result;
         chi2 += dlt * dlt / stats[M + i];
     }
@@ -600,8 +700,15 @@ cvg_status cvg_context_create(int device, void *stream, cvg_context *out)
     if (e != cudaSuccess) { delete c; return fail(CVG_ERR_CUDA, cudaGetErrorString(e)); }
     c->n_sm = prop.multiProcessorCount;
     c->smem_optin = (int)prop.sharedMemPerBlockOptin;
+    c->smem_per_sm = (int)prop.sharedMemPerMultiprocessor;
     c->cc_major = prop.major;
     c->cc_minor = prop.minor;
+    {   // arenas kept for reuse: up to CVG_ARENA_CACHE_MB (default 1/8 of the device)
+        const char *cap = std::getenv("CVG_ARENA_CACHE_MB");
+        c->arena_cache_cap = cap ? (size_t)std::strtoull(cap, nullptr, 10) << 20 : prop.totalGlobalMem / 8;
+        const char *poison = std::getenv("CVG_ARENA_POISON");
+        c->arena_poison = poison && *poison && *poison != '0';
+    }
     char arch[32];
     std::snprintf(arch, sizeof(arch), "sm_%d%da", prop.major, prop.minor);
     c->arch = arch;
@@ -618,11 +725,23 @@ cvg_status cvg_context_create(int device, void *stream, cvg_context *out)
     return CVG_OK;
 }
 
+cvg_status cvg_context_trim(cvg_context ctx)
+{
+    if (!ctx) return fail(CVG_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lock(ctx->arena_mu);
+    cudaSetDevice(ctx->device);
+    for (auto &kv : ctx->arena_cache) cudaFree(kv.second);
+    ctx->arena_cache.clear();
+    ctx->arena_cached = 0;
+    return CVG_OK;
+}
+
 cvg_status cvg_context_destroy(cvg_context ctx)
 {
     if (!ctx) return CVG_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cvg_context_trim(ctx);
     for (auto &kv : ctx->libs) cudaLibraryUnload(kv.second);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
@@ -648,6 +767,24 @@ cvg_status cvg_compile_integrand(cvg_context ctx, const char *source, int32_t n_
     f->has_grad = has_grad ? 1 : 0;
     // Kernels are compiled on first use (run creation), per precision and tile
     // shape; source errors are reported there with the NVRTC log.
+    *out = f;
+    return CVG_OK;
+}
+
+cvg_status cvg_compile_integrand_ptx(cvg_context ctx, const char *source, const char *ptx,
+                                     int32_t n_dim, cvg_integrand *out)
+{
+    if (!ctx || !ptx || !out) return fail(CVG_ERR_INVALID, "NULL argument");
+    if (n_dim < 1 || n_dim > 32) return fail(CVG_ERR_INVALID, "n_dim must be in [1, 32]");
+    if (!std::strstr(ptx, ".func")) return fail(CVG_ERR_INVALID, "ptx defines no device function");
+    auto *f = new cvg_integrand_s();
+    f->ctx = ctx;
+    f->source = (source && *source)
+                    ? std::string(source)
+                    : std::string("extern \"C\" __device__ int integrand(double* ret, double* x);\n");
+    f->link_ptx = ptx;
+    f->dim = n_dim;
+    f->abi = CVG_ABI_NUMBA;
     *out = f;
     return CVG_OK;
 }
@@ -739,7 +876,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     };
     size_t total = 0;
     for (auto &s : segs) total += (s.bytes + 255) & ~(size_t)255;
-    e = cudaMalloc(&r->arena, total);
+    e = cvg_internal_arena_alloc(ctx, total, &r->arena, &r->arena_bytes);
     if (e != cudaSuccess) {
         delete r;
         return fail(CVG_ERR_NOMEM, std::string("cudaMalloc of the run arena (") +
@@ -809,7 +946,7 @@ cvg_status cvg_run_destroy(cvg_run r)
     if (r->ev_fork) cudaEventDestroy(r->ev_fork);
     if (r->ev_join) cudaEventDestroy(r->ev_join);
     if (r->ubuf) cudaFree(r->ubuf);
-    if (r->arena) cudaFree(r->arena);
+    if (r->arena) cvg_internal_arena_free(r->ctx, r->arena, r->arena_bytes);
     delete r;
     return CVG_OK;
 }
@@ -864,11 +1001,9 @@ cvg_status cvg_run_result(cvg_run r, cvg_result *out, double *it_res, double *it
 {
     if (!r || !out) return fail(CVG_ERR_INVALID, "NULL argument");
     CK(cudaSetDevice(r->ctx->device));
-    cvg_acc_dev acc;
     const int M = r->p.max_it;
-    std::vector<double> stats(2 * (size_t)M);
-    CK(cudaMemcpyAsync(&acc, r->acc, sizeof(acc), cudaMemcpyDeviceToHost, r->ctx->stream));
-    CK(cudaMemcpyAsync(stats.data(), r->stats, sizeof(double) * 2 * M, cudaMemcpyDeviceToHost,
+    std::vector<double> stats(3 * (size_t)M);
+    CK(cudaMemcpyAsync(stats.data(), r->stats, sizeof(double) * 3 * M, cudaMemcpyDeviceToHost,
                        r->ctx->stream));
     CKS(check_status(r));
     std::memset(out, 0, sizeof(*out));
@@ -877,7 +1012,9 @@ cvg_status cvg_run_result(cvg_run r, cvg_result *out, double *it_res, double *it
     out->n_strat = r->n_strat;
     out->n_intervals = r->p.n_intervals;
     out->n_cubes = r->n_cubes;
-    out->tot_nevals = (int64_t)acc.tot_nevals;
+    double nev = 0.0;   // samples of every iteration done (also those of an imported state)
+    for (int i = 0; i < done; ++i) nev += stats[2 * (size_t)M + i];
+    out->tot_nevals = (int64_t)nev;
     out->seed = r->p.seed;
     out->gpu_thr = r->p.gpu_thr;
     out->precision = r->p.precision;
@@ -972,8 +1109,18 @@ cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes)
     case CVG_BUF_WEIGHTS: dst = r->weights; need = sizeof(double) * D * N; break;
     case CVG_BUF_COUNTS: dst = r->counts; need = sizeof(cvg_u32) * D * N; break;
     case CVG_BUF_THETA: dst = r->theta; need = sizeof(double) * r->f->n_params; break;
-    case CVG_BUF_ITERATION: dst = r->iteration; need = sizeof(cvg_u32); break;
+    case CVG_BUF_ITERATION:
+        dst = r->iteration;
+        need = sizeof(cvg_u32);
+        if (host && bytes == need) {   // the loop continues from this iteration
+            const cvg_u32 it = *(const cvg_u32 *)host;
+            if (it > (cvg_u32)r->p.max_it) return fail(CVG_ERR_INVALID, "iteration beyond max_it");
+            r->it_done = (int)it;
+        }
+        break;
     case CVG_BUF_SCALE_EXP: dst = r->scale_exp; need = sizeof(int); break;
+    case CVG_BUF_STATS: dst = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
+    case CVG_BUF_BIN_EXP: dst = r->bin_exp; need = sizeof(int) * ((size_t)D * N + 1); break;
     case CVG_BUF_UNIFORMS: {
         if (bytes == 0) { r->replay = false; return CVG_OK; }
         if (!host || bytes % (sizeof(float) * D)) return fail(CVG_ERR_INVALID, "uniforms: [S][dim] floats");
@@ -1179,7 +1326,7 @@ cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int
     std::string all;
     cvg_status st = CVG_OK;
     for (int g = 0; g <= (has_grad ? 1 : 0) && st == CVG_OK; ++g) {
-        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi, 1024};
+        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi, 1024, 1};
         std::vector<char> cubin;
         std::string l;
         st = nvrtc_cubin(make_source(f, k), nvrtc_options(arch), cubin, l);

@@ -98,6 +98,92 @@ __device__ double integrand(double* x, const double* th) { return cvg_corner(x, 
 __device__ float integrand(float* x, const float* th) { return cvg_corner(x, th); }
 """
 
+# The reference's integrand library (src/commons/functions.cu:5-111) as
+# templates over double and float, in the reference's operation order.  The
+# reference's float-precision steps are kept: fabsf in roosarnold, sqrtf(12)
+# in hellekalek.
+REFLIB_NAMES = ("linear", "roosarnold", "morokoffcalfisch", "hellekalek", "ridge", "expon",
+                "cosin", "dirichlet", "gaussian", "sinexp", "one")
+
+_REFLIB = r"""
+template <typename T> __device__ __forceinline__ T cvg_ref_linear(const T* x, int n) {
+    T f = (T)0;
+    for (int i = 0; i < n; i++) f += x[i];
+    return f;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_roosarnold(const T* x, int n) {
+    const T f = (T)1 / (T)n;
+    T aux = (T)0;
+    for (int i = 0; i < n; i++) aux += (T)fabsf((float)((T)4 * x[i] - (T)2));
+    return f * aux;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_morokoffcalfisch(const T* x, int n) {
+    T f = (T)1;
+    for (int i = 0; i < n; i++) f *= pow(x[i], (T)1 / (T)n);
+    f *= pow((T)1 + (T)1 / (T)n, (T)n);
+    return f;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_hellekalek(const T* x, int n) {
+    T f = (T)1;
+    for (int i = 0; i < n; i++) f *= ((x[i] - (T)0.5) / (T)sqrtf(12.0f));
+    return f;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_ridge(const T* x, int n) {
+    const int N = 1000;
+    const T norm = pow((T)100 / (T)3.14159265358979323846, (T)2) / (T)N;
+    T f = (T)0;
+    for (int i = 0; i < N; i++) {
+        const T x0 = (T)i / ((T)N - (T)1);
+        T dx2 = (T)0;
+        for (int j = 0; j < n; j++) { const T a = x[j] - x0; dx2 += a * a; }
+        f += exp((T)-100 * dx2);
+    }
+    return f * norm;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_expon(const T* x, int n) {
+    T f = (T)0;
+    for (int i = 0; i < n; i++) f += x[i] * x[i];
+    return exp(-f);
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_cosin(const T* x, int n) {
+    T f = (T)1;
+    for (int i = 0; i < n; i++) f *= cos(x[i]);
+    return f;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_dirichlet(const T* x, int n) {
+    const T alpha = (T)5;
+    const T b = pow(tgamma(alpha), (T)n) / tgamma(alpha * (T)n);
+    T f = (T)1;
+    for (int i = 0; i < n; i++) f *= pow(x[i], alpha - (T)1);
+    return f / b;
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_gaussian(const T* x, int n) {
+    const T sigma2 = (T)0.0001, mu = (T)0.5;
+    T f = (T)0;
+    for (int i = 0; i < n; i++) { const T a = x[i] - mu; f += a * a; }
+    return exp((T)-0.5 * f / sigma2) / pow((T)2 * (T)3.14159265358979323846 * sigma2, (T)n / (T)2);
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_sinexp(const T* x, int n) {
+    (void)n;
+    return sin(x[0]) + exp(x[1]);
+}
+template <typename T> __device__ __forceinline__ T cvg_ref_one(const T* x, int n) {
+    (void)x; (void)n;
+    return (T)1;
+}
+"""
+
+
+def reflib_source(name):
+    """Integrand source for one function of the reference's library (the
+    choice config.cuh makes with `return ridge(x, n_dim);`)."""
+    if name not in REFLIB_NAMES:
+        raise ValueError("unknown reference function %r" % (name,))
+    return _REFLIB + (
+        "__device__ double integrand(double* x) { return cvg_ref_%s(x, cvg_n_dim); }\n"
+        "__device__ float integrand(float* x) { return cvg_ref_%s(x, cvg_n_dim); }\n" % (name, name))
+
+
 CONST_ONE = r"""
 template <typename T> __device__ __forceinline__ T cvg_one(T* x) { (void)x; return (T)1; }
 __device__ double integrand(double* x) { return cvg_one(x); }

@@ -7,8 +7,10 @@ same keyword arguments with the same meanings and defaults, same result tuple
 
 Differences, by design:
   * ``device_function`` is CUDA C++ source defining ``integrand`` (compiled by
-    NVRTC inside libcuvegas), or a numba CUDA device function when numba is
-    installed (it must then be given as source: numba's PTX is not linked);
+    NVRTC inside libcuvegas); or a numba CUDA device function ``f(x) -> float``
+    (needs numba), compiled to PTX with numba's own ABI-naming option and
+    linked into the fill; or such PTX text (a function ``integrand`` with
+    numba's ABI, ``int integrand(double* ret, double* x)``);
   * ``multi_gpu``, ``multi_cpu``, ``gpu_num``, ``cpu_num`` and ``gpu_thr`` are
     accepted and reported but change nothing: one GPU, no CPU mapping fallback;
   * ``precision='fp32'`` selects the FP32 evaluation with compensated
@@ -48,13 +50,52 @@ def _domain_source(source, domain, n_dim, abi):
         "    return cvg_user_integrand(x) * (T)%r;\n}\n" % (fmt(start), fmt(rng), vol))
 
 
+def _is_ptx(obj):
+    return isinstance(obj, str) and ".version" in obj and ".func" in obj
+
+
+def _is_numba(obj):
+    return type(obj).__module__.startswith("numba") and hasattr(obj, "py_func")
+
+
+def _numba_ptx(fn, abi_name):
+    """PTX of a numba device function f(x: float64*) -> float64 with numba's
+    ABI under the given name (numba's abi_info option; the reference renames
+    the function by editing the PTX text, python_wrapper.py:48-59)."""
+    from numba import cuda, types
+    sig = types.float64(types.CPointer(types.float64))
+    ptx, _ = cuda.compile(fn.py_func, sig, device=True, abi="numba",
+                          abi_info={"abi_name": abi_name}, output="ptx", cc=(10, 3))
+    return ptx
+
+
+def _ptx_domain_source(domain, n_dim, inner):
+    """numba-ABI `integrand` that remaps [0,1]^d to `domain` and calls `inner`."""
+    start = [float(domain[i][0]) for i in range(n_dim)]
+    rng = [float(domain[i][1]) - float(domain[i][0]) for i in range(n_dim)]
+    vol = float(np.prod(rng))
+    fmt = lambda v: ", ".join(repr(x) for x in v)
+    return ('extern "C" __device__ int %s(double* ret, double* x);\n'
+            'extern "C" __device__ int integrand(double* ret, double* x) {\n'
+            '    const double a[] = {%s};\n    const double r[] = {%s};\n'
+            '    double y[cvg_n_dim];\n'
+            '    for (int i = 0; i < cvg_n_dim; ++i) y[i] = x[i] * r[i] + a[i];\n'
+            '    const int s = %s(ret, y);\n    *ret *= %r;\n    return s;\n}\n'
+            % (inner, fmt(start), fmt(rng), inner, vol))
+
+
+def _trivial_domain(domain, n_dim):
+    return domain is None or all(float(domain[i][0]) == 0.0 and float(domain[i][1]) == 1.0
+                                 for i in range(n_dim))
+
+
 def _as_source(device_function):
     if isinstance(device_function, str):
         return device_function, L.ABI_NATIVE
     if isinstance(device_function, tuple) and len(device_function) == 2:
         return device_function[0], int(device_function[1])
-    raise TypeError("device_function must be CUDA C++ source text defining `integrand` "
-                    "(numba device functions are not linked by this build)")
+    raise TypeError("device_function must be CUDA C++ source text defining `integrand`, "
+                    "a numba CUDA device function, or numba-ABI PTX")
 
 
 def integrate(device_function, n_dim, domain=None, n_evals=1000000, max_it=20, skip=5,
@@ -68,14 +109,29 @@ def integrate(device_function, n_dim, domain=None, n_evals=1000000, max_it=20, s
     if n_strat is None:
         n_eval_it = n_evals // max_it
         n_strat = int(math.pow((n_eval_it / 4.0), 1.0 / n_dim))
-    source, abi = _as_source(device_function)
-    if domain is not None:
-        source = _domain_source(source, domain, n_dim, abi)
     prec = {"fp64": L.PREC_FP64, "fp32": L.PREC_FP32}[precision]
     if theta is not None and not n_params:
         n_params = len(theta)
     ctx = runtime.default_context(device)
-    f = ctx.integrand(source, n_dim, n_params=n_params, abi=abi)
+    if _is_numba(device_function) or _is_ptx(device_function):
+        if prec != L.PREC_FP64:
+            raise ValueError("numba integrands are FP64: precision must be 'fp64'")
+        remap = not _trivial_domain(domain, n_dim)
+        if _is_numba(device_function):
+            inner = "cvg_numba_user" if remap else "integrand"
+            ptx = _numba_ptx(device_function, inner)
+        else:
+            if remap:
+                raise ValueError("a PTX `integrand` cannot be wrapped for domain remapping; "
+                                 "compile it under another abi_name and pass a numba function")
+            ptx = device_function
+        f = ctx.integrand_ptx(ptx, n_dim, source=_ptx_domain_source(domain, n_dim, inner)
+                              if remap else None)
+    else:
+        source, abi = _as_source(device_function)
+        if domain is not None:
+            source = _domain_source(source, domain, n_dim, abi)
+        f = ctx.integrand(source, n_dim, n_params=n_params, abi=abi)
     p = runtime.make_params(n_dim, n_evals, max_it, skip=skip, n_intervals=n_intervals,
                             n_strat=n_strat, alpha=alpha, beta=beta, seed=seed, precision=prec,
                             flags=L.FLAG_GRAPH if graph else 0, max_batch_size=batch_size,

@@ -37,6 +37,10 @@ class Context:
         except Exception:
             pass
 
+    def trim(self):
+        """Free the device arenas kept from destroyed runs and batches."""
+        L.check(self._lib.cvg_context_trim(self.handle))
+
     def measure_peak(self, kind):
         v = C.c_double()
         L.check(self._lib.cvg_measure_peak(self.handle, int(kind), C.byref(v)))
@@ -47,6 +51,15 @@ class Context:
         f = self._integrands.get(key)
         if f is None:
             f = Integrand(self, source, n_dim, n_params, has_grad, abi)
+            self._integrands[key] = f
+        return f
+
+    def integrand_ptx(self, ptx, n_dim, source=None):
+        """Integrand given as PTX with the numba ABI (cvg_compile_integrand_ptx)."""
+        key = ("ptx", ptx, source, int(n_dim))
+        f = self._integrands.get(key)
+        if f is None:
+            f = Integrand(self, source or "", n_dim, abi=L.ABI_NUMBA, ptx=ptx)
             self._integrands[key] = f
         return f
 
@@ -70,15 +83,19 @@ def default_context(device=None):
 class Integrand:
     """A JIT-compiled integrand (cvg_compile_integrand)."""
 
-    def __init__(self, ctx, source, n_dim, n_params=0, has_grad=False, abi=L.ABI_NATIVE):
+    def __init__(self, ctx, source, n_dim, n_params=0, has_grad=False, abi=L.ABI_NATIVE, ptx=None):
         self.ctx = ctx
-        self.source = source
+        self.source = source + (ptx or "")
         self.n_dim = int(n_dim)
         self.n_params = int(n_params)
         self.has_grad = bool(has_grad)
         h = C.c_void_p()
-        L.check(ctx._lib.cvg_compile_integrand(ctx.handle, source.encode(), self.n_dim, int(abi),
-                                               self.n_params, int(self.has_grad), C.byref(h)))
+        if ptx is not None:
+            L.check(ctx._lib.cvg_compile_integrand_ptx(ctx.handle, source.encode() if source else None,
+                                                       ptx.encode(), self.n_dim, C.byref(h)))
+        else:
+            L.check(ctx._lib.cvg_compile_integrand(ctx.handle, source.encode(), self.n_dim, int(abi),
+                                                   self.n_params, int(self.has_grad), C.byref(h)))
         self.handle = h
 
     def close(self):
@@ -227,6 +244,59 @@ class Run:
             a = np.ascontiguousarray(arr, dtype=_BUF_DTYPES[buf]).ravel()
         L.check(self._lib.cvg_run_set(self.handle, int(buf), a.ctypes.data_as(C.c_void_p),
                                       a.nbytes))
+
+    # ---- state export / import (checkpoint, resume, warm start) ----------
+    def export_state(self):
+        """The loop's state between iterations: grid, hypercube allocation,
+        iteration counter and per-iteration estimates (plus, in the FP32 form,
+        the f*jac scale and the per-bin exponent table).  A run created with
+        the same dimension, bins and hypercubes continues from it with
+        import_state; with FLAG_NO_ADAPT it integrates on the trained map."""
+        self.sync()
+        st = {"n_dim": self.info.n_dim, "n_intervals": self.info.n_intervals,
+              "n_cubes": self.info.n_cubes, "precision": self.params.precision,
+              "max_it": self.params.max_it,
+              "x_edges": self.get(L.BUF_X_EDGES), "nh": self.get(L.BUF_NH),
+              "iteration": int(self.get(L.BUF_ITERATION)[0]), "stats": self.get(L.BUF_STATS)}
+        if self.params.precision == L.PREC_FP32:
+            st["scale_exp"] = int(self.get(L.BUF_SCALE_EXP)[0])
+            st["bin_exp"] = self.get(L.BUF_BIN_EXP)
+        return st
+
+    def import_state(self, st, resume=True):
+        """Load a state from export_state.  resume=True also takes over the
+        iteration counter and the estimates, so the weighted mean continues
+        over the earlier iterations (the Philox stream continues too);
+        resume=False keeps this run's own counter and estimates (a warm start
+        on the trained map)."""
+        info = self.info
+        if (int(st["n_dim"]), int(st["n_intervals"]), int(st["n_cubes"])) != \
+                (info.n_dim, info.n_intervals, info.n_cubes):
+            raise ValueError("state of a run with another dimension, bin count or hypercubes")
+        self.set(L.BUF_X_EDGES, st["x_edges"])
+        self.set(L.BUF_NH, st["nh"])
+        if self.params.precision == L.PREC_FP32 and "bin_exp" in st:
+            self.set(L.BUF_SCALE_EXP, np.array([st["scale_exp"]], dtype=np.int32))
+            self.set(L.BUF_BIN_EXP, st["bin_exp"])
+        if resume:
+            it = int(st["iteration"])
+            if it > self.params.max_it:
+                raise ValueError("state is at iteration %d, this run has max_it %d"
+                                 % (it, self.params.max_it))
+            old = np.asarray(st["stats"], dtype=np.float64).reshape(3, -1)
+            stats = np.zeros((3, self.params.max_it))
+            stats[:, :it] = old[:, :it]
+            self.set(L.BUF_STATS, stats)
+            self.set(L.BUF_ITERATION, np.array([it], dtype=np.uint32))
+
+    def save_state(self, path):
+        st = self.export_state()
+        np.savez(path, **{k: np.asarray(v) for k, v in st.items()})
+
+    @staticmethod
+    def load_state(path):
+        with np.load(path) as z:
+            return {k: (z[k] if z[k].ndim else z[k].item()) for k in z.files}
 
     def grad(self, it=L.IT_CURRENT):
         g = np.zeros(self.f.n_params)

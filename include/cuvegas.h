@@ -101,6 +101,11 @@ const char *cvg_version(void);
  * or a cudaStream_t owned by the caller. */
 cvg_status cvg_context_create(int device, void *stream, cvg_context *out);
 cvg_status cvg_context_destroy(cvg_context ctx);
+/* Free the device arenas the context keeps from destroyed runs and batches
+ * for reuse (the cache holds up to CVG_ARENA_CACHE_MB, default 1/8 of the
+ * device; no counterpart in the reference, which allocates and frees every
+ * buffer inside each call, cuda_wrapper.cu:392-451, 779-851). */
+cvg_status cvg_context_trim(cvg_context ctx);
 
 /* JIT-compile an integrand from CUDA C++ source (replaces numba PTX + the
  * cuLink step, python_wrapper.py:48-61 and cuda_wrapper.cu:221-286).  The
@@ -111,6 +116,16 @@ cvg_status cvg_context_destroy(cvg_context ctx);
 cvg_status cvg_compile_integrand(cvg_context ctx, const char *source, int32_t n_dim,
                                  int32_t abi, int32_t n_params, int32_t has_grad,
                                  cvg_integrand *out);
+/* Integrand given as PTX (numba's ABI, the device ABI the reference links:
+ * a function `integrand` with `int integrand(double* ret, double* x)`,
+ * vegas_cuda/src/vegas_cuda_extension/cuda_kernel.cu:7 and python_wrapper.py:48-59,
+ * e.g. numba.cuda.compile(..., abi="numba", abi_info={"abi_name": "integrand"})).
+ * `source` (may be NULL) is CUDA C++ compiled with the fill; when given it
+ * must declare or wrap `extern "C" __device__ int integrand(double*, double*)`.
+ * Each fill module is compiled relocatable and linked with the PTX (nvJitLink).
+ * FP64 form only. */
+cvg_status cvg_compile_integrand_ptx(cvg_context ctx, const char *source, const char *ptx,
+                                     int32_t n_dim, cvg_integrand *out);
 cvg_status cvg_integrand_release(cvg_integrand f);
 
 /* Whole integration, the drop-in for integrate_cuda
@@ -147,15 +162,16 @@ enum {
     CVG_BUF_COUNTS = 6,      /* uint32 [dim][N]          get/set                  */
     CVG_BUF_DH = 7,          /* double [n_cubes]         get                      */
     CVG_BUF_THETA = 8,       /* double [n_params]        get/set                  */
-    CVG_BUF_ITERATION = 9,   /* uint32 [1]               get/set                  */
+    CVG_BUF_ITERATION = 9,   /* uint32 [1]               get/set (set: the loop continues from
+                                this iteration; Philox counter word 2)                  */
     CVG_BUF_UNIFORMS = 10,   /* float  [S][dim]          set: replay these uniforms in
                                 the next fills instead of Philox (parity tests); 0 bytes
                                 switches back                                         */
-    CVG_BUF_STATS = 11,      /* double [3][max_it]       get: I_it, sigma2_it, samples_it */
+    CVG_BUF_STATS = 11,      /* double [3][max_it]       get/set: I_it, sigma2_it, samples_it */
     CVG_BUF_SCALE_EXP = 12,  /* int32  [1]               get/set: FP32 form carries f*jac
                                 scaled by 2^-k (k chosen by a pilot, then updated each
                                 iteration) so (f*jac)^2 stays in float range             */
-    CVG_BUF_BIN_EXP = 13     /* int32  [dim*N+1]         get: FP32 form, binary exponent of
+    CVG_BUF_BIN_EXP = 13     /* int32  [dim*N+1]         get/set: FP32 form, binary exponent of
                                 each bin's expected per-sample (f*jac)^2 for the next fill
                                 (unscaled; set by the pilot, then by each refinement); the
                                 last entry is the k of the last fill                      */

@@ -43,7 +43,9 @@ void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 /* Integrands                                                                */
 /* ------------------------------------------------------------------------ */
 
-/* Reference integrand library, src/commons/functions.cu:5-111, restated.    */
+/* Reference integrand library, src/commons/functions.cu:5-111, restated:   */
+/* 0 linear, 1 roosarnold, 2 morokoffcalfisch, 3 hellekalek, 4 ridge,       */
+/* 5 expon, 6 cosin, 7 dirichlet, 8 gaussian, 9 sinexp, 10 one.             */
 /* The float-precision quirks of the reference (fabsf in roosarnold,         */
 /* sqrtf in hellekalek) are kept.                                            */
 static double reflib(int idx, const double *x, int n)
@@ -81,6 +83,31 @@ static double reflib(int idx, const double *x, int n)
         }
         return f * norm;
     }
+    case 5: /* expon, functions.cu:62-69 */
+        f = 0.0;
+        for (int i = 0; i < n; i++) f += x[i] * x[i];
+        return exp(-f);
+    case 6: /* cosin, functions.cu:71-78 */
+        f = 1.0;
+        for (int i = 0; i < n; i++) f *= cos(x[i]);
+        return f;
+    case 7: { /* dirichlet, functions.cu:80-89 (alpha = 5) */
+        const double alpha = 5.0;
+        const double b = pow(tgamma(alpha), n) / tgamma(alpha * n);
+        f = 1.0;
+        for (int i = 0; i < n; i++) f *= pow(x[i], alpha - 1.0);
+        return f / b;
+    }
+    case 8: { /* gaussian, functions.cu:91-101 (sigma^2 = 1e-4, mu = 0.5) */
+        const double sigma2 = 0.0001, mu = 0.5;
+        f = 0.0;
+        for (int i = 0; i < n; i++) { const double a = x[i] - mu; f += a * a; }
+        return exp(-0.5 * f / sigma2) / pow(2.0 * M_PI * sigma2, n / 2.0);
+    }
+    case 9: /* sinexp, functions.cu:103-106 (needs n >= 2) */
+        return sin(x[0]) + exp(x[1]);
+    case 10: /* one, functions.cu:108-111 */
+        return 1.0;
     default:
         return 0.0;
     }

@@ -297,3 +297,29 @@ def test_state_checks(ctx):
         with pytest.raises(L.CuvegasError) as e:
             r.iterate(1)
         assert e.value.status == L.ERR_STATE
+
+
+def test_reused_arena_gives_identical_runs(monkeypatch):
+    """Destroyed runs leave their device arena to the context and the next run
+    of a similar size takes it over.  With CVG_ARENA_POISON every arena handed
+    out is filled with 0xFF bytes (NaN doubles), so a buffer a run reads
+    without initialising it shows up as NaN or as a different result.  Runs
+    agree to summation order (FP64 atomics add shared runs in any order)."""
+    monkeypatch.setenv("CVG_ARENA_POISON", "1")
+    pctx = runtime.Context(0)
+
+    def once(n_it, prec):
+        with make_run(pctx, I.GAUSS, 4, n_it, 5, N=256, seed=9, prec=prec) as r:
+            r.iterate(5)
+            res, it_res, it_sig = r.result()
+            return np.concatenate([it_res, it_sig, [res.result, res.error]]), r.get(L.BUF_X_EDGES)
+    try:
+        for prec in (L.PREC_FP64, L.PREC_FP32):
+            a = once(300000, prec)            # fresh, poisoned allocation
+            once(500000, prec)                # other data left in the cached arena
+            b = once(300000, prec)            # reuses it, poisoned again
+            assert np.all(np.isfinite(a[0])) and np.all(np.isfinite(a[1]))
+            np.testing.assert_allclose(b[0], a[0], rtol=1e-12)
+            np.testing.assert_allclose(b[1], a[1], rtol=1e-12, atol=1e-15)
+    finally:
+        pctx.close()
