@@ -379,6 +379,7 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         a.scale_exp = p.precision == CVG_PREC_FP32 ? h.scale_exp : nullptr;
         a.scale_ss = p.precision == CVG_PREC_FP32 ? h.scale_ss : nullptr;
         a.bin_exp = p.precision == CVG_PREC_FP32 ? h.bin_exp : nullptr;
+        a.hist_state = nullptr;   // batched fills always keep fixed-point bin sums
         a.max_tiles = h.max_tiles;
         a.seed = p.seed;
         a.instance = insts[i].instance;
@@ -413,6 +414,8 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         r.skip = p.skip;
         r.max_it = p.max_it;
         r.fast_pow = p.precision == CVG_PREC_FP32 ? 1 : 0;
+        r.hist_state = nullptr;
+        r.dim = D;
         r.adapt = (p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
         cvg_refine_args &q = hq[i];
         q.x_edges = h.x_edges;

@@ -37,6 +37,8 @@ struct cvg_fill_args {
     cvg_u32 *status;              // error bits
     int *scale_exp;               // FP32 form: f*jac is scaled by 2^-scale_exp (may be null)
     double *scale_ss;             // FP32-form pilot: sum of (f*jac)^2 over its samples
+    cvg_u32 *hist_state;          // FP32 form: [0] 1 = fixed-point bin sums in this fill,
+                                  // [1] rare updates the fill counts (or null)
     int *bin_exp;                 // FP32 form: [dim][N] binary exponent of each bin's expected
                                   // per-sample (f*jac)^2 (unscaled); [dim*N] = the scale
                                   // exponent k of the last fill (null for FP64)

@@ -141,13 +141,14 @@ template <int D, typename T> CVG_D constexpr bool cvg_hist_fixed()
     return sizeof(T) == 4 && D <= CVG_HIST_FIX_MAX_DIM;
 }
 
+// Returns 1 when the update took a rare path (a wrap or a large weight).
 template <bool FIX>
-CVG_D void cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
+CVG_D cvg_u32 cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
 {
     if (!FIX) {
         atomicAdd(hw + i, w);
         atomicAdd(hc + i, 1u);
-        return;
+        return 0u;
     }
     const cvg_u32 old = atomicAdd(hc + i, 1u);
     const int e = (int)old >> 24;                             // this bin's scale exponent
@@ -155,10 +156,14 @@ CVG_D void cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
     if (s < 8388608.0f) {   // round-to-nearest integer by a 2^23 add (no conversion instruction)
         const cvg_u32 q = __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u;
         const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
-        if (o + q < o) atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
-    } else {
-        atomicAdd(gw + i, cvg_f2d(w));
+        if (o + q < o) {
+            atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
+            return 1u;
+        }
+        return 0u;
     }
+    atomicAdd(gw + i, cvg_f2d(w));
+    return 1u;
 }
 // Fixed-point update of bin i without branches: returns 1 if w did not fit
 // (the caller adds it to the global FP64 sum), 2 if the word wrapped (the
@@ -179,10 +184,11 @@ CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, flo
     if (rare & 2u) atomicAdd(gw + i, __hiloint2double((1039 + ((int)hc[i] >> 24)) << 20, 0));
 }
 template <bool FIX>
-CVG_D void cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
+CVG_D cvg_u32 cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
 {
     atomicAdd(hw + i, w);
     atomicAdd(hc + i, 1u);
+    return 0u;
 }
 // Bin sum and count of a shared-memory histogram entry, in the units of the
 // global histogram.
@@ -207,6 +213,76 @@ CVG_D cvg_u32 cvg_hist_word(const cvg_fill_args &a, int i, int kx)
     int e = a.bin_exp ? a.bin_exp[i] - 2 * kx : 0;
     e = e < -100 ? -100 : (e > 100 ? 100 : e);
     return (cvg_u32)e << 24;
+}
+
+// Add a thread's run sums of cube c to the global per-cube sums.  When every
+// lane of a full, converged warp holds a single run of the same cube (a
+// hypercube with hundreds of samples or more, as the reallocation produces
+// for peaked integrands), the warp first combines its runs -- in
+// double-float for the FP32 form -- so one atomic pair replaces 32 on the
+// same two addresses.
+CVG_D void cvg_two_sum(float a, float b, float &s, float &e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+CVG_D void cvg_df_acc(float &h, float &l, float oh, float ol)
+{
+    float s, e;
+    cvg_two_sum(h, oh, s, e);
+    e += l + ol;
+    h = s + e;
+    l = e - (h - s);
+}
+CVG_D void cvg_run_to_global(const cvg_fill_args &a, cvg_u32 c, const cvg_acc<float> &a1,
+                             const cvg_acc<float> &a2, int kx, bool whole)
+{
+    const unsigned m = __activemask();
+    bool same = false;
+    if (m == 0xffffffffu) {   // every lane executes both collectives
+        const cvg_u32 c0 = __shfl_sync(m, c, 0);
+        same = __all_sync(m, whole && c == c0);
+    }
+    if (same) {
+        float h1 = a1.s, l1 = -a1.k, h2 = a2.s, l2 = -a2.k;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh1 = __shfl_xor_sync(m, h1, o), ol1 = __shfl_xor_sync(m, l1, o);
+            const float oh2 = __shfl_xor_sync(m, h2, o), ol2 = __shfl_xor_sync(m, l2, o);
+            cvg_df_acc(h1, l1, oh1, ol1);
+            cvg_df_acc(h2, l2, oh2, ol2);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(&a.JF[c], cvg_to_double_scaled(h1, kx) + cvg_to_double_scaled(l1, kx));
+            atomicAdd(&a.JF2[c], cvg_to_double_scaled(h2, 2 * kx) + cvg_to_double_scaled(l2, 2 * kx));
+        }
+        return;
+    }
+    atomicAdd(&a.JF[c], cvg_to_double_scaled(a1.value_t(), kx));
+    atomicAdd(&a.JF2[c], cvg_to_double_scaled(a2.value_t(), 2 * kx));
+}
+CVG_D void cvg_run_to_global(const cvg_fill_args &a, cvg_u32 c, const cvg_acc<double> &a1,
+                             const cvg_acc<double> &a2, int, bool whole)
+{
+    const unsigned m = __activemask();
+    double v1 = a1.value(), v2 = a2.value();
+    bool same = false;
+    if (m == 0xffffffffu) {   // every lane executes both collectives
+        const cvg_u32 c0 = __shfl_sync(m, c, 0);
+        same = __all_sync(m, whole && c == c0);
+    }
+    if (same) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v1 += __shfl_xor_sync(m, v1, o);
+            v2 += __shfl_xor_sync(m, v2, o);
+        }
+        if ((threadIdx.x & 31) == 0) { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
+        return;
+    }
+    atomicAdd(&a.JF[c], v1);
+    atomicAdd(&a.JF2[c], v2);
 }
 
 // Stratum offsets coord_d * dy of cube c (digit d of c in base n_strat, least
@@ -275,7 +351,7 @@ struct cvg_fill_ctx {
 
 // Load theta and the grid into shared memory, clear the bin histograms and
 // set the per-instance constants.  The caller synchronises afterwards.
-template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD>
+template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD, bool FIX>
 CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                           cvg_fill_ctx<T> &cx)
 {
@@ -304,7 +380,7 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     if (H) {
         for (int i = tid; i < D * N; i += BS) {
             sm.hw[i] = (T)0;
-            sm.hc[i] = cvg_hist_word<cvg_hist_fixed<D, T>()>(a, i, cx.kx);
+            sm.hc[i] = cvg_hist_word<FIX>(a, i, cx.kx);
         }
         // the refinement turns this fill's bin sums (units 2^-2k) back into
         // unscaled exponents for the next fill's table
@@ -316,10 +392,10 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
 // One tile: samples [tile*TS, min((tile+1)*TS, S)).  Returns false (and sets a
 // status bit) if the tile map is inconsistent; uniform across the block.
 template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
-          int NI>
+          int NI, bool FIX>
 CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                          const cvg_fill_ctx<T> &cx, cvg_u64 tile, cvg_u64 n_tiles, cvg_u64 S,
-                         cvg_acc<T> *gacc)
+                         cvg_acc<T> *gacc, cvg_u32 &nrare)
 {
     constexpr int PP = P > 0 ? P : 1;
     constexpr int NB = (D + 3) / 4;
@@ -429,13 +505,13 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
             } else {
                 const T jf = (T)F::f(x, sm.th) * jac;
                 const T jf2 = jf * jf;
-                if constexpr (H && cvg_hist_fixed<D, T>()) {
+                if constexpr (H && FIX) {
 #ifdef CVG_FILL_LOWREG
                     // held to 64 registers (2 CTAs per SM): branches keep the
                     // dimensions' updates apart and fewer values live
 #pragma unroll
                     for (int d = 0; d < D; ++d)
-                        cvg_hist_add<true>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
+                        nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
 #else
                     // fixed-point bin sums; a wrap or a large weight (rare) is
                     // handled behind a single branch per dimension
@@ -443,7 +519,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                     for (int d = 0; d < D; ++d) {
                         const int i = d * N + bin[d];
                         const cvg_u32 rare = cvg_hist_add_fix(sm.hw, sm.hc, i, jf2);
-                        if (rare) cvg_hist_rare(sm.hc, a.weights, i, rare, jf2);
+                        if (rare) { cvg_hist_rare(sm.hc, a.weights, i, rare, jf2); ++nrare; }
                     }
 #endif
                 } else {
@@ -468,10 +544,12 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 #pragma unroll
                 for (int p = 0; p < PP; ++p) gacc[p].add(ag[p] * sc);
             } else {
-                const double v1 = cvg_to_double_scaled(a1.value_t(), cx.kx);
-                const double v2 = cvg_to_double_scaled(a2.value_t(), 2 * cx.kx);
-                if (cstart >= l0 && next == lend) { a.JF[c] = v1; a.JF2[c] = v2; }
-                else { atomicAdd(&a.JF[c], v1); atomicAdd(&a.JF2[c], v2); }
+                if (cstart >= l0 && next == lend) {
+                    a.JF[c] = cvg_to_double_scaled(a1.value_t(), cx.kx);
+                    a.JF2[c] = cvg_to_double_scaled(a2.value_t(), 2 * cx.kx);
+                } else {
+                    cvg_run_to_global(a, c, a1, a2, cx.kx, run == lend - l0);
+                }
             }
         }
     }
@@ -481,7 +559,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 
 // Add the CTA's shared-memory bin histograms to the global FP64/u32 ones;
 // with reset, clear them for more samples (scale exponents kept).
-template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD, int NI>
+template <int D, typename T, int BS, bool ESM, bool HSM, int P, bool GRAD, int NI, bool FIX>
 CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                           bool reset = false)
 {
@@ -489,9 +567,9 @@ CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     __syncthreads();
     const int N = NI > 0 ? NI : a.n_intervals;
     for (int i = threadIdx.x; i < D * N; i += BS) {
-        const cvg_u32 cn = cvg_hist_count<cvg_hist_fixed<D, T>()>(sm.hc[i]);
+        const cvg_u32 cn = cvg_hist_count<FIX>(sm.hc[i]);
         if (cn) {
-            const double w = cvg_hist_value<cvg_hist_fixed<D, T>()>(sm.hw, sm.hc, i);
+            const double w = cvg_hist_value<FIX>(sm.hw, sm.hc, i);
             if (w != 0.0) atomicAdd(&a.weights[i], w);
             atomicAdd(&a.counts[i], cn);
             if (reset) { sm.hw[i] = (T)0; sm.hc[i] -= cn; }
@@ -500,46 +578,60 @@ CVG_D void cvg_fill_flush(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     __syncthreads();
 }
 
+// Rare histogram updates (wraps, large weights) of a CTA, added to the
+// instance's count once; the reallocation's finish step reads it to choose
+// the next fill's histogram form.
+CVG_D void cvg_fill_count_rare(const cvg_fill_args &a, cvg_u32 nrare)
+{
+    if (!a.hist_state) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrare += __shfl_down_sync(0xffffffffu, nrare, o);
+    if ((threadIdx.x & 31) == 0 && nrare) atomicAdd(&a.hist_state[1], nrare);
+}
+
+// FP32 form: fixed-point bin sums when the instance's state says so (the
+// per-bin exponents predicted the weights well in the last fill), float
+// atomics otherwise.  Uniform across the launch.
+template <int D, typename T>
+CVG_D bool cvg_fill_use_fixed(const cvg_fill_args &a)
+{
+    return cvg_hist_fixed<D, T>() && (!a.hist_state || a.hist_state[0] != 0u);
+}
+
 // Persistent single-instance fill: this CTA takes tiles blockIdx.x,
 // blockIdx.x + gridDim.x, ...
 template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
-          int NI = 0>
-CVG_D void cvg_fill_body(const cvg_fill_args &a)
+          int NI, bool FIX>
+CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
     constexpr int PP = P > 0 ? P : 1;
     const int tid = threadIdx.x;
-    const cvg_u64 S = a.nh_sum[a.n_cubes];
     const int TS = a.tile_samples;
-    cvg_u64 n_tiles = (S + (cvg_u64)TS - 1) / (cvg_u64)TS;
-    if (n_tiles > a.max_tiles) {   // never produced by the reallocation; keep accesses in bounds
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
-        n_tiles = a.max_tiles;
-    }
-    if ((cvg_u64)blockIdx.x >= n_tiles) return;
-
     cvg_fill_smem<D, T, ESM, HSM, P, GRAD> sm;
     sm.carve(cvg_smem, a.n_intervals, TS);
     cvg_fill_ctx<T> cx;
-    cvg_fill_setup<D, T, BS, ESM, HSM, P, GRAD>(a, sm, cx);
+    cvg_fill_setup<D, T, BS, ESM, HSM, P, GRAD, FIX>(a, sm, cx);
     cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
 #pragma unroll
     for (int p = 0; p < PP; ++p) gacc[p].reset();
     __syncthreads();
 
+    cvg_u32 nrare = 0;
     cvg_u64 since = 0;   // samples in the shared histograms since their last flush
     for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
         if (since + (cvg_u64)TS > CVG_HIST_MAX_RUN) {
-            cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI>(a, sm, true);
+            cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm, true);
             since = 0;
         }
         since += (cvg_u64)TS;
-        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI>(a, sm, cx, tile, n_tiles, S,
-                                                                      gacc))
+        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX>(a, sm, cx, tile, n_tiles,
+                                                                           S, gacc, nrare))
             break;
     }
 
-    cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI>(a, sm);
+    cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm);
+    if (FIX) cvg_fill_count_rare(a, nrare);
     if (GRAD) {
         const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
@@ -558,6 +650,28 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
     }
 }
 
+template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
+          int NI = 0>
+CVG_D void cvg_fill_body(const cvg_fill_args &a)
+{
+    const cvg_u64 S = a.nh_sum[a.n_cubes];
+    const int TS = a.tile_samples;
+    cvg_u64 n_tiles = (S + (cvg_u64)TS - 1) / (cvg_u64)TS;
+    if (n_tiles > a.max_tiles) {   // never produced by the reallocation; keep accesses in bounds
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
+        n_tiles = a.max_tiles;
+    }
+    if ((cvg_u64)blockIdx.x >= n_tiles) return;
+    if constexpr (cvg_hist_fixed<D, T>() && HSM && !GRAD) {
+        if (cvg_fill_use_fixed<D, T>(a))
+            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, true>(a, S, n_tiles);
+        else
+            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles);
+    } else {
+        cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Batched fill: many independent integrals (different dimensions and sample
 // counts) in one persistent launch.  Tiles of all instances are numbered
@@ -568,6 +682,7 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 // the dimensions present; DISP::fn<D> is the integrand of dimension D.
 // ---------------------------------------------------------------------------
 template <int V> struct cvg_int { static constexpr int value = V; };
+template <bool V> struct cvg_bool { static constexpr bool value = V; };
 
 
 template <typename T, int BS, class DISP, int NI = 0>
@@ -593,25 +708,34 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
         DISP::run(b.dims[i], [&](auto Dc, auto Pc) {
             constexpr int D = decltype(Dc)::value, P = decltype(Pc)::value;
             using F = typename DISP::template fn<D>;
-            cvg_fill_smem<D, T, true, true, P, false> sm;
-            sm.carve(cvg_smem, a.n_intervals, a.tile_samples);
-            cvg_fill_ctx<T> cx;
-            cvg_fill_setup<D, T, BS, true, true, P, false>(a, sm, cx);
-            __syncthreads();
-            const cvg_u64 S = a.nh_sum[a.n_cubes];
-            const cvg_u64 nt = b.tile_base[i + 1] - tb;
-            cvg_u64 since = 0;
-            for (cvg_u64 lt = t - tb; lt < te - tb; ++lt) {
-                if (since + (cvg_u64)a.tile_samples > CVG_HIST_MAX_RUN) {
-                    cvg_fill_flush<D, T, BS, true, true, P, false, NI>(a, sm, true);
-                    since = 0;
+            auto range = [&](auto Fx) {
+                constexpr bool FIX = decltype(Fx)::value;
+                cvg_fill_smem<D, T, true, true, P, false> sm;
+                sm.carve(cvg_smem, a.n_intervals, a.tile_samples);
+                cvg_fill_ctx<T> cx;
+                cvg_fill_setup<D, T, BS, true, true, P, false, FIX>(a, sm, cx);
+                __syncthreads();
+                const cvg_u64 S = a.nh_sum[a.n_cubes];
+                const cvg_u64 nt = b.tile_base[i + 1] - tb;
+                cvg_u32 nrare = 0;
+                cvg_u64 since = 0;
+                for (cvg_u64 lt = t - tb; lt < te - tb; ++lt) {
+                    if (since + (cvg_u64)a.tile_samples > CVG_HIST_MAX_RUN) {
+                        cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm, true);
+                        since = 0;
+                    }
+                    since += (cvg_u64)a.tile_samples;
+                    if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX>(
+                            a, sm, cx, lt, nt, S, nullptr, nrare))
+                        break;
                 }
-                since += (cvg_u64)a.tile_samples;
-                if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI>(a, sm, cx, lt, nt,
-                                                                                 S, nullptr))
-                    break;
-            }
-            cvg_fill_flush<D, T, BS, true, true, P, false, NI>(a, sm);
+                cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm);
+                if (FIX) cvg_fill_count_rare(a, nrare);
+            };
+            // one histogram form per dimension here: a second copy of every
+            // dimension's loop made the batched kernel spill (it is held to 64
+            // registers per thread)
+            range(cvg_bool<cvg_hist_fixed<D, T>()>{});
         });
         t = te;
     }

@@ -109,6 +109,7 @@ struct cvg_run_s {
     int *scale_exp = nullptr;
     double *scale_ss = nullptr;
     int *bin_exp = nullptr;
+    cvg_u32 *hist_state = nullptr;
     cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
@@ -254,7 +255,18 @@ std::vector<std::string> nvrtc_options(const std::string &arch)
     std::vector<std::string> o = {"--gpu-architecture=" + arch, "-std=c++17", "-default-device",
                                   "-lineinfo"};
     const char *extra = std::getenv("CVG_NVRTC_EXTRA");   // e.g. --ptxas-options=-v
-    if (extra && *extra) o.push_back(extra);
+    if (extra && *extra) {                                 // space-separated options
+        std::string opt;
+        for (const char *c = extra;; ++c) {
+            if (*c == ' ' || *c == '\0') {
+                if (!opt.empty()) o.push_back(opt);
+                opt.clear();
+                if (!*c) break;
+            } else {
+                opt += *c;
+            }
+        }
+    }
     return o;
 }
 
@@ -408,6 +420,10 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.max_it = r->p.max_it;
     a.fast_pow = r->p.precision == CVG_PREC_FP32 ? 1 : 0;
     a.adapt = (r->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
+    a.hist_state = r->p.precision == CVG_PREC_FP32 ? r->hist_state : nullptr;
+    a.dim = r->f->dim;
+    a.rare_shift = 10;    // fixed point while rare updates stay below 1 in 1024
+    a.hist_min_it = 2;    // float bin sums in the fill after the first reallocation
     return a;
 }
 
@@ -445,6 +461,7 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
     a.scale_ss = r->p.precision == CVG_PREC_FP32 ? r->scale_ss : nullptr;
     a.bin_exp = r->p.precision == CVG_PREC_FP32 ? r->bin_exp : nullptr;
+    a.hist_state = r->p.precision == CVG_PREC_FP32 ? r->hist_state : nullptr;
     a.max_tiles = r->max_tiles;
     a.seed = r->p.seed;
     a.instance = r->p.instance;
@@ -630,7 +647,9 @@ void cvg_internal_arena_free(cvg_context ctx, void *p, size_t bytes)
 
 int cvg_internal_fill_minb(cvg_context ctx, int block, size_t smem)
 {
-    const int by_smem = ctx && ctx->smem_per_sm > 0 ? (int)(ctx->smem_per_sm / (smem + 1024)) : 1;
+    // without a context (compile checks): the 228 KB of an sm_100/sm_103 SM
+    const size_t per_sm = ctx && ctx->smem_per_sm > 0 ? (size_t)ctx->smem_per_sm : 233472u;
+    const int by_smem = (int)(per_sm / (smem + 1024));
     const int by_regs = 65536 / (block * 64);
     return std::max(1, std::min(by_smem, by_regs));
 }
@@ -870,6 +889,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->scale_exp, sizeof(int)},
         {(void **)&r->scale_ss, sizeof(double)},
         {(void **)&r->bin_exp, sizeof(int) * ((size_t)D * N + 1)},
+        {(void **)&r->hist_state, 2 * sizeof(cvg_u32)},
         {(void **)&r->done, 2 * sizeof(cvg_u32)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
@@ -911,6 +931,10 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->iteration, 0, sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->status, 0, sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->done, 0, 2 * sizeof(cvg_u32), st));
+    {   // the first fill uses fixed-point bin sums with the pilot's exponent table
+        const cvg_u32 hs[2] = {1u, 0u};
+        CK(cudaMemcpyAsync(r->hist_state, hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+    }
     CK(cudaMemsetAsync(r->stats, 0, sizeof(double) * 3 * p.max_it, st));
     CK(cudaMemsetAsync(r->grad, 0, sizeof(double) * std::max(1, f->n_params), st));
     if (f->n_params > 0)
@@ -1071,6 +1095,7 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     case CVG_BUF_STATS: src = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
     case CVG_BUF_SCALE_EXP: src = r->scale_exp; need = sizeof(int); break;
     case CVG_BUF_BIN_EXP: src = r->bin_exp; need = sizeof(int) * ((size_t)D * N + 1); break;
+    case CVG_BUF_HIST_STATE: src = r->hist_state; need = 2 * sizeof(cvg_u32); break;
     default: return fail(CVG_ERR_INVALID, "unknown buffer");
     }
     if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
@@ -1121,6 +1146,7 @@ cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes)
     case CVG_BUF_SCALE_EXP: dst = r->scale_exp; need = sizeof(int); break;
     case CVG_BUF_STATS: dst = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;
     case CVG_BUF_BIN_EXP: dst = r->bin_exp; need = sizeof(int) * ((size_t)D * N + 1); break;
+    case CVG_BUF_HIST_STATE: dst = r->hist_state; need = 2 * sizeof(cvg_u32); break;
     case CVG_BUF_UNIFORMS: {
         if (bytes == 0) { r->replay = false; return CVG_OK; }
         if (!host || bytes % (sizeof(float) * D)) return fail(CVG_ERR_INVALID, "uniforms: [S][dim] floats");
@@ -1141,7 +1167,11 @@ cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes)
     }
     if (!host || bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
     CK(cudaMemcpyAsync(dst, host, need, cudaMemcpyHostToDevice, st));
-    if (buf == CVG_BUF_X_EDGES) CK(cvg_launch_grid32(r->x_edges, r->x_edges32, D * (N + 1), st));
+    if (buf == CVG_BUF_X_EDGES) {
+        CK(cvg_launch_grid32(r->x_edges, r->x_edges32, D * (N + 1), st));
+        // the exponent table belongs to the old grid: float bin sums next
+        CK(cudaMemsetAsync(r->hist_state, 0, 2 * sizeof(cvg_u32), st));
+    }
     CK(cudaStreamSynchronize(st));
     return CVG_OK;
 }
@@ -1326,7 +1356,15 @@ cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int
     std::string all;
     cvg_status st = CVG_OK;
     for (int g = 0; g <= (has_grad ? 1 : 0) && st == CVG_OK; ++g) {
-        variant_key k{n_dim, precision, 256, 1, g ? 0 : 1, 0, n_params, g, abi, 1024, 1};
+        // the default launch shape of a run (512 threads, 8 samples each,
+        // 1024 bins, grid and histograms in shared memory when they fit)
+        const int tsz = precision == CVG_PREC_FP32 ? 4 : 8;
+        variant_key k{n_dim, precision, 512, 1, g ? 0 : 1, 0, n_params, g, abi, 1024, 1};
+        if (cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, 4096, n_params, 512) > 232448)
+            k.hsm = 0;
+        k.minb = cvg_internal_fill_minb(nullptr, 512,
+                                        cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, 4096,
+                                                            n_params, 512));
         std::vector<char> cubin;
         std::string l;
         st = nvrtc_cubin(make_source(f, k), nvrtc_options(arch), cubin, l);

@@ -64,6 +64,7 @@ void cvg_internal_arena_free(cvg_context ctx, void *p, size_t bytes);
 // blocks): as many as shared memory allows, but never a register cap below
 // 64 per thread.
 int cvg_internal_fill_minb(cvg_context ctx, int block, size_t smem);
+
 // FP32-form scale exponent k from the pilot: 2^k near the rms of f*jac
 // (sum of squares ss over n samples), raised so that the largest seen
 // |f*jac| (binary exponent emax) stays below 2^60 after scaling.

@@ -340,6 +340,17 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
             acc->used += 1;
         }
         if (!isfinite(r) || !isfinite(s)) atomicOr(a.status, CVG_KSTAT_NONFINITE);
+        if (a.hist_state) {
+            // FP32 form: fixed-point bin sums in the next fill only from the third
+            // iteration on (the first reallocation of a peaked integrand moves
+            // the samples far from what the exponent table predicts) and only
+            // while rare updates stayed below 1 in 1024
+            const double rare = (double)a.hist_state[1];
+            const bool ok = (int)it + 1 >= a.hist_min_it &&
+                            ldexp(rare, a.rare_shift) <= (double)S * (double)a.dim;
+            a.hist_state[0] = ok ? 1u : 0u;
+            a.hist_state[1] = 0u;
+        }
         *a.iteration = it + 1;
     }
 }

@@ -48,6 +48,11 @@ struct cvg_realloc_args {
     int fast_pow;           // 1: FP32 form (compensated FP32 per cube, FP64 sums); d_h is
                             //    then (var)^beta without the cube-volume factor V^(2 beta)
     int adapt;              // 0: keep nh (no reallocation), still accumulate results
+    cvg_u32 *hist_state;    // FP32 form: the fill's histogram form (see cvg_fill_args), chosen
+                            // here for the next fill; or null
+    int dim;
+    int rare_shift;         // fixed point stays while rare updates <= dim*samples / 2^rare_shift
+    int hist_min_it;        // first iteration that may use fixed point again after iteration 0
 };
 
 struct cvg_refine_args {

