@@ -111,9 +111,13 @@ CVG_D cvg_u32x4 cvg_philox(cvg_u32 c0, cvg_u32 c1, cvg_u32 c2, cvg_u32 c3, cvg_u
 //  float : (2*(r>>9)+1) * 2^-24, built by exponent splicing (no int->float convert)
 //  double: (r + 0.5) * 2^-32, built the same way; both exact.
 template <typename T> CVG_D T cvg_uniform(cvg_u32 r);
+// FP32: the top 23 bits as the significand of t in [1, 2) (the same bits the
+// FP64 uniform starts with, so both forms draw nearly the same points),
+// u = t - (1 - 2^-24) = m 2^-23 + 2^-24 (exact), in (0, 1).
+CVG_D float cvg_uniform_t(cvg_u32 r) { return __uint_as_float((r >> 9) + 0x3F800000u); }
 template <> CVG_D float cvg_uniform<float>(cvg_u32 r)
 {
-    return __uint_as_float(0x3F800000u | (r >> 9)) - 0.99999994039535522461f;
+    return cvg_uniform_t(r) - 0.99999994039535522461f;
 }
 template <> CVG_D double cvg_uniform<double>(cvg_u32 r)
 {

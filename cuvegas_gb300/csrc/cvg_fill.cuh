@@ -106,6 +106,14 @@ CVG_D int cvg_bin(float z, int N, float fNm1, float &frac)
     frac = z - bf;
     return __float_as_int(bf + C) - 0x4B000000;
 }
+// Same for z known to be positive (Philox samples): no lower clamp.
+CVG_D int cvg_bin_pos(float z, float fNm1, float &frac)
+{
+    const float C = 8388608.0f;
+    const float bf = fminf(__fadd_rd(z, C) - C, fNm1);
+    frac = z - bf;
+    return __float_as_int(bf + C) - 0x4B000000;
+}
 CVG_D int cvg_bin(double z, int N, double, double &frac)
 {
     int b = (int)z;
@@ -285,22 +293,22 @@ CVG_D void cvg_run_to_global(const cvg_fill_args &a, cvg_u32 c, const cvg_acc<do
     atomicAdd(&a.JF2[c], v2);
 }
 
-// Stratum offsets coord_d * dy of cube c (digit d of c in base n_strat, least
-// significant first: src/main.cu:43-47); cvg_cube_next steps to cube c+1
-// like an odometer.
+// Stratum offsets coord_d * dy - sh of cube c (digit d of c in base n_strat,
+// least significant first: src/main.cu:43-47); cvg_cube_next steps to cube
+// c+1 like an odometer.  sh = 0 gives the reference's coord * dy.
 template <int D, typename T>
-CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, int *coord, T *cdy)
+CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, T sh, int *coord, T *cdy)
 {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const cvg_u32 q = c / ns;
         coord[d] = (int)(c - q * ns);
-        cdy[d] = (T)coord[d] * dy;
+        cdy[d] = (T)coord[d] * dy - sh;
         c = q;
     }
 }
 template <int D, typename T>
-CVG_D void cvg_cube_next(int ns, T dy, int *coord, T *cdy)
+CVG_D void cvg_cube_next(int ns, T dy, T sh, int *coord, T *cdy)
 {
     bool carry = true;
 #pragma unroll
@@ -309,7 +317,7 @@ CVG_D void cvg_cube_next(int ns, T dy, int *coord, T *cdy)
             const int v = coord[d] + 1;
             carry = v == ns;
             coord[d] = carry ? 0 : v;
-            cdy[d] = (T)coord[d] * dy;
+            cdy[d] = (T)coord[d] * dy - sh;
         }
     }
 }
@@ -432,9 +440,15 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
         int cstart = starts[ci];
         int next = starts[ci + 1];
         cvg_u32 j = (cvg_u32)(l0 - cstart);
+        // FP32 form with Philox samples: z = y*N is formed directly from the
+        // uniform's significand t in [1,2): z = t*(N/ns) + (coord - (1-2^-24))*(N/ns),
+        // one FMA instead of shift, subtract, FMA and multiply
+        constexpr bool ZF = sizeof(T) == 4 && !REPLAY;
+        const T zs = ZF ? dy * fN : dy;
+        const T zsh = ZF ? (T)0.99999994039535522461 * zs : (T)0;
         int coord[D];
         T cdy[D];
-        cvg_cube_offsets<D, T>(c, (cvg_u32)ns, dy, coord, cdy);
+        cvg_cube_offsets<D, T>(c, (cvg_u32)ns, zs, zsh, coord, cdy);
         const int lend = min(l0 + spt, lend_tile);
 
         cvg_acc<T> a1, a2;
@@ -464,7 +478,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 }
                 do {  // empty cubes (never produced by the reallocation) are skipped
                     ++ci; ++c;
-                    cvg_cube_next<D, T>(ns, dy, coord, cdy);
+                    cvg_cube_next<D, T>(ns, zs, zsh, coord, cdy);
                     cstart = next;
                     next = starts[ci + 1];
                 } while (l >= next && ci < K - 2);
@@ -482,13 +496,20 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 for (int q = 0; q < 4; ++q) {
                     const int d = 4 * bk + q;
                     if (d >= D) break;
-                    T u;
-                    if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
-                    else u = cvg_uniform<T>(q == 0 ? r4.x : q == 1 ? r4.y : q == 2 ? r4.z : r4.w);
-                    const T y = cvg_fma(u, dy, cdy[d]);
-                    const T z = y * fN;
-                    T frac;
-                    const int b = cvg_bin(z, N, fNm1, frac);
+                    T z, frac;
+                    int b;
+                    if constexpr (ZF) {
+                        const cvg_u32 r = q == 0 ? r4.x : q == 1 ? r4.y : q == 2 ? r4.z : r4.w;
+                        z = fmaf(cvg_uniform_t(r), zs, cdy[d]);
+                        b = cvg_bin_pos(z, fNm1, frac);
+                    } else {
+                        T u;
+                        if (REPLAY) u = (T)a.ubuf[(base + (cvg_u64)l) * D + d];
+                        else u = cvg_uniform<T>(q == 0 ? r4.x : q == 1 ? r4.y : q == 2 ? r4.z : r4.w);
+                        const T y = cvg_fma(u, dy, cdy[d]);
+                        z = y * fN;
+                        b = cvg_bin(z, N, fNm1, frac);
+                    }
                     const T e0 = G[d * (N + 1) + b];
                     const T e1 = G[d * (N + 1) + b + 1];
                     const T dx = e1 - e0;
