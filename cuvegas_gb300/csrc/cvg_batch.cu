@@ -184,6 +184,7 @@ cvg_batch_args batch_args(const cvg_batch_s *b)
     a.dims = b->d_dims;
     a.tile_base = b->d_tile_base;
     a.n_inst = b->n;
+    cvg_philox_schedule(b->p.seed, a.keys);
     return a;
 }
 
@@ -390,6 +391,7 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         a.spt = b->spt;
         a.n_params = h.n_params;
         a.v_cubes = h.v_cubes;
+        cvg_philox_schedule(p.seed, a.keys);
         cvg_realloc_args &r = hr[i];
         r.nh_sum = h.nh_sum;
         r.JF = h.JF;

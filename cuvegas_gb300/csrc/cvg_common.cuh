@@ -19,6 +19,18 @@ typedef long long cvg_i64;
 #define CVG_KSTAT_BAD_TILE 1u      // tile map inconsistent with nh_sum
 #define CVG_KSTAT_NONFINITE 2u     // a non-finite per-cube estimate was seen
 
+// Philox4x32-10 key schedule of one seed: round r uses (k0 + r*0x9E3779B9,
+// k1 + r*0xBB67AE85).  Kept in the kernel arguments (constant bank), so the
+// rounds read their key words directly instead of recomputing them per call.
+struct cvg_philox_keys { cvg_u32 k[2][10]; };
+CVG_HD void cvg_philox_schedule(cvg_u64 seed, cvg_philox_keys &ks)
+{
+    for (int r = 0; r < 10; ++r) {
+        ks.k[0][r] = (cvg_u32)seed + (cvg_u32)r * 0x9E3779B9u;
+        ks.k[1][r] = (cvg_u32)(seed >> 32) + (cvg_u32)r * 0xBB67AE85u;
+    }
+}
+
 // Arguments of one fill launch.  Layout is shared between host and device;
 // only fixed-width scalar types and pointers.
 struct cvg_fill_args {
@@ -53,6 +65,7 @@ struct cvg_fill_args {
     int n_params;
     int pad0;
     double v_cubes;               // volume of one hypercube
+    cvg_philox_keys keys;         // key schedule of seed
 };
 
 // Arguments of one batched fill launch.
@@ -61,6 +74,7 @@ struct cvg_batch_args {
     const int *dims;              // [n_inst]
     const cvg_u64 *tile_base;     // [n_inst + 1] first global tile of each instance
     int n_inst;
+    cvg_philox_keys keys;         // key schedule of the common seed
 };
 
 CVG_HD cvg_u64 cvg_align16(cvg_u64 x) { return (x + 15ull) & ~15ull; }
@@ -101,6 +115,21 @@ CVG_D cvg_u32x4 cvg_philox(cvg_u32 c0, cvg_u32 c1, cvg_u32 c2, cvg_u32 c3, cvg_u
         const cvg_u64 p1 = (cvg_u64)0xCD9E8D57u * c2;
         const cvg_u32 n0 = (cvg_u32)(p1 >> 32) ^ c1 ^ k0;
         const cvg_u32 n2 = (cvg_u32)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (cvg_u32)p1; c2 = n2; c3 = (cvg_u32)p0;
+    }
+    cvg_u32x4 o; o.x = c0; o.y = c1; o.z = c2; o.w = c3;
+    return o;
+}
+// The same with the key schedule precomputed (cvg_philox_schedule).
+CVG_D cvg_u32x4 cvg_philox_ks(cvg_u32 c0, cvg_u32 c1, cvg_u32 c2, cvg_u32 c3,
+                              const cvg_philox_keys &ks)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const cvg_u64 p0 = (cvg_u64)0xD2511F53u * c0;
+        const cvg_u64 p1 = (cvg_u64)0xCD9E8D57u * c2;
+        const cvg_u32 n0 = (cvg_u32)(p1 >> 32) ^ c1 ^ ks.k[0][r];
+        const cvg_u32 n2 = (cvg_u32)(p0 >> 32) ^ c3 ^ ks.k[1][r];
         c0 = n0; c1 = (cvg_u32)p1; c2 = n2; c3 = (cvg_u32)p0;
     }
     cvg_u32x4 o; o.x = c0; o.y = c1; o.z = c2; o.w = c3;

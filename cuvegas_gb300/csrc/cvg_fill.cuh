@@ -403,7 +403,7 @@ template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, boo
           int NI, bool FIX>
 CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                          const cvg_fill_ctx<T> &cx, cvg_u64 tile, cvg_u64 n_tiles, cvg_u64 S,
-                         cvg_acc<T> *gacc, cvg_u32 &nrare)
+                         cvg_acc<T> *gacc, cvg_u32 &nrare, const cvg_philox_keys &keys)
 {
     constexpr int PP = P > 0 ? P : 1;
     constexpr int NB = (D + 3) / 4;
@@ -491,7 +491,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 #pragma unroll
             for (int bk = 0; bk < NB; ++bk) {   // 4 dimensions per Philox call
                 cvg_u32x4 r4;
-                if (!REPLAY) r4 = cvg_philox(j, c, cx.it, (cvg_u32)bk | cx.c3, cx.k0, cx.k1);
+                if (!REPLAY) r4 = cvg_philox_ks(j, c, cx.it, (cvg_u32)bk | cx.c3, keys);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int d = 4 * bk + q;
@@ -647,7 +647,7 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
         }
         since += (cvg_u64)TS;
         if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX>(a, sm, cx, tile, n_tiles,
-                                                                           S, gacc, nrare))
+                                                                           S, gacc, nrare, a.keys))
             break;
     }
 
@@ -747,7 +747,7 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
                     }
                     since += (cvg_u64)a.tile_samples;
                     if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX>(
-                            a, sm, cx, lt, nt, S, nullptr, nrare))
+                            a, sm, cx, lt, nt, S, nullptr, nrare, b.keys))
                         break;
                 }
                 cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm);

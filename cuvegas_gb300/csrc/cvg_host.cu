@@ -472,6 +472,7 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.spt = r->spt;
     a.n_params = r->f->n_params;
     a.v_cubes = r->v_cubes;
+    cvg_philox_schedule(r->p.seed, a.keys);
     return a;
 }
 
