@@ -32,10 +32,11 @@ def test_resume_from_checkpoint_equals_one_run(ctx, prec, tmp_path):
         res, it_res, _ = r.result()
         edges = r.get(L.BUF_X_EDGES)
     # same Philox words, grids and allocations: equal up to the summation order
-    # of the FP64 atomics
-    np.testing.assert_allclose(it_res, ref_it, rtol=1e-9)
-    np.testing.assert_allclose(edges, ref_edges, rtol=1e-7, atol=1e-9)
-    assert abs(res.result - ref.result) <= 1e-9 * abs(ref.result)
+    # of the FP64 atomics (which can move a sample across a bin edge after a
+    # few iterations: ~1e-6 of an estimate; a wrong resume differs by ~1e-3)
+    np.testing.assert_allclose(it_res, ref_it, rtol=2e-5)
+    np.testing.assert_allclose(edges, ref_edges, rtol=1e-6, atol=1e-8)
+    assert abs(res.result - ref.result) <= 2e-5 * abs(ref.result)
     assert res.tot_nevals == ref.tot_nevals
 
 
