@@ -17,7 +17,7 @@ import threading
 from . import _lib as L
 from . import runtime
 
-CANDIDATES = [(256, 8), (512, 4), (512, 8), (512, 16), (1024, 4), (1024, 8)]
+CANDIDATES = [(256, 16), (512, 8), (512, 12), (512, 16), (1024, 4), (1024, 8)]
 _lock = threading.Lock()
 
 

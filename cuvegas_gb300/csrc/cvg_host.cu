@@ -859,6 +859,26 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     r->spt = p.spt > 0 ? p.spt : 8;
     if (r->block % 32 || r->block > 1024) { delete r; return fail(CVG_ERR_INVALID, "block must be a multiple of 32, <= 1024"); }
     if (r->spt < 1 || r->spt > 256) { delete r; return fail(CVG_ERR_INVALID, "spt must be in [1, 256]"); }
+    if (p.spt <= 0) {
+        // default: 16 samples per thread (half the per-tile staging of 8;
+        // measured 4 % faster at d = 8 and d = 16) unless the larger
+        // cube-start table costs a CTA per SM
+        const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8, N = p.n_intervals;
+        auto ctas = [&](int spt) {
+            const int TS = r->block * spt;
+            for (auto &o : {std::pair<int, int>{1, 1}, {0, 1}, {1, 0}, {0, 0}}) {
+                const cvg_u64 b = cvg_fill_smem_bytes(D, N, tsz, o.first, o.second, 0, TS,
+                                                      f->n_params, r->block);
+                if (b <= (cvg_u64)ctx->smem_optin) return (int)(ctx->smem_per_sm / (b + 1024));
+            }
+            return 0;
+        };
+        // ... and unless the iteration has too few tiles to give every CTA of
+        // the persistent grid several (small runs keep more, smaller tiles)
+        const cvg_u64 tiles16 = s_max / ((cvg_u64)r->block * 16);
+        const int c16 = ctas(16);
+        if (c16 >= ctas(8) && c16 > 0 && tiles16 >= 4ull * (cvg_u64)c16 * ctx->n_sm) r->spt = 16;
+    }
     r->TS = r->block * r->spt;
     r->max_tiles = (s_max + r->TS - 1) / r->TS + 1;
     r->nb = cvg_realloc_blocks(r->n_cubes);
