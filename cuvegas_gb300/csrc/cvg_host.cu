@@ -1110,7 +1110,20 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     case CVG_BUF_JF2: src = r->JF2; need = sizeof(double) * r->n_cubes; break;
     case CVG_BUF_WEIGHTS: src = r->weights; need = sizeof(double) * D * N; break;
     case CVG_BUF_COUNTS: src = r->counts; need = sizeof(cvg_u32) * D * N; break;
-    case CVG_BUF_DH: src = r->dh; need = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_DH:
+        src = r->dh;
+        need = sizeof(double) * r->n_cubes;
+        if (r->p.precision == CVG_PREC_FP32) {   // stored as float by the FP32 form
+            if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch");
+            std::vector<float> tmp(r->n_cubes);
+            CK(cudaMemcpyAsync(tmp.data(), r->dh, sizeof(float) * tmp.size(), cudaMemcpyDeviceToHost,
+                               r->ctx->stream));
+            CK(cudaStreamSynchronize(r->ctx->stream));
+            double *o = (double *)host;
+            for (size_t c = 0; c < tmp.size(); ++c) o[c] = tmp[c];
+            return CVG_OK;
+        }
+        break;
     case CVG_BUF_THETA: src = r->theta; need = sizeof(double) * r->f->n_params; break;
     case CVG_BUF_ITERATION: src = r->iteration; need = sizeof(cvg_u32); break;
     case CVG_BUF_STATS: src = r->stats; need = sizeof(double) * 3 * r->p.max_it; break;

@@ -206,7 +206,7 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
     const cvg_u64 *__restrict__ nhs = a.nh_sum;
     double *__restrict__ JF = a.JF;
     double *__restrict__ JF2 = a.JF2;
-    double *__restrict__ DH = a.dh;
+    float *__restrict__ DH = reinterpret_cast<float *>(a.dh);   // FP32 form: d_h as float
     // issue every load of this thread's cubes before any store
     cvg_u64 s0[RIPT], s1[RIPT];
     double j1[RIPT], j2[RIPT];
@@ -253,7 +253,7 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
             const float y = dh - kd, t = sd + y;
             kd = (t - sd) - y; sd = t;
         }
-        DH[c] = f2d_bits(dh);
+        DH[c] = dh;
     }
     // warp reduction in FP32 (double-float for the estimate)
     float v = sv - kv, d = sd - kd;
@@ -361,35 +361,41 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
 // mode 0: nh from the damped variances (updateNh, src/main.cu:173-187)
 // mode 1: nh_new already holds the counts (initialisation / state import)
 // mode 2: FP32 form, nh = floor(d_h * n_eval_it / sum d_h) in FP32
-__device__ __forceinline__ void k3_count_dev(const cvg_realloc_args &a, int mode, const unsigned blk)
+// mode 0: n_h from the FP64 d_h (reference conversion); 1: n_h given in
+// nh_new; 2: n_h from the FP32 form's float d_h, scaled.
+template <int MODE>
+__device__ __forceinline__ void k3_count_mode(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ cvg_u64 wtot[RB / 32];
     const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     double dsum = 0.0, n_it = 0.0;
     float scale = 0.f;
-    if (mode == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
-    if (mode == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;   // round the total down
+    if (MODE == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
+    if (MODE == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;   // round the total down
     cvg_u64 tot = 0;
-    double dhv[RIPT];
+    double dhv[MODE == 0 ? RIPT : 1];
+    float dhf[MODE == 2 ? RIPT : 1];
+    const float *dh32 = reinterpret_cast<const float *>(a.dh);
 #pragma unroll
     for (int k = 0; k < RIPT; ++k) {   // issue the loads first
         const cvg_u32 c = base + k * RB + threadIdx.x;
-        dhv[k] = (mode != 1 && c < a.n_cubes) ? a.dh[c] : 0.0;
+        if (MODE == 0) dhv[k] = c < a.n_cubes ? a.dh[c] : 0.0;
+        if (MODE == 2) dhf[k] = c < a.n_cubes ? dh32[c] : 0.f;
     }
 #pragma unroll
     for (int k = 0; k < RIPT; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
         cvg_u32 nh;
-        if (mode == 0) {
+        if (MODE == 0) {
             const double f = dhv[k] / dsum;
             const double x = f * n_it;
             // (int) conversion of the reference: NaN -> 0, saturating above
             int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
             nh = ns < 2 ? 2u : (cvg_u32)ns;
             a.nh_new[c] = nh;
-        } else if (mode == 2) {
-            const float x = d2f_bits(dhv[k]) * scale;
+        } else if (MODE == 2) {
+            const float x = dhf[k] * scale;
             const int ns = (x >= 0.f && x < 2147483520.f) ? (int)x : (x >= 2147483520.f ? 2147483520 : 0);
             nh = ns < 2 ? 2u : (cvg_u32)ns;
             a.nh_new[c] = nh;
@@ -407,6 +413,13 @@ __device__ __forceinline__ void k3_count_dev(const cvg_realloc_args &a, int mode
         for (int w = 0; w < RB / 32; ++w) t += wtot[w];
         a.bsums[blk] = t;
     }
+}
+
+__device__ __forceinline__ void k3_count_dev(const cvg_realloc_args &a, int mode, const unsigned blk)
+{
+    if (mode == 0) k3_count_mode<0>(a, blk);
+    else if (mode == 1) k3_count_mode<1>(a, blk);
+    else k3_count_mode<2>(a, blk);
 }
 
 __global__ void __launch_bounds__(RB) k3_count(cvg_realloc_args a, int mode)

@@ -160,7 +160,8 @@ enum {
     CVG_BUF_JF2 = 4,         /* double [n_cubes]         get/set                  */
     CVG_BUF_WEIGHTS = 5,     /* double [dim][N]          get/set                  */
     CVG_BUF_COUNTS = 6,      /* uint32 [dim][N]          get/set                  */
-    CVG_BUF_DH = 7,          /* double [n_cubes]         get                      */
+    CVG_BUF_DH = 7,          /* double [n_cubes]         get (FP32 form: kept as float,
+                                widened on the way out)                               */
     CVG_BUF_THETA = 8,       /* double [n_params]        get/set                  */
     CVG_BUF_ITERATION = 9,   /* uint32 [1]               get/set (set: the loop continues from
                                 this iteration; Philox counter word 2)                  */

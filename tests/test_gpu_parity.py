@@ -32,7 +32,8 @@ def relerr(a, b):
 
 
 @pytest.mark.parametrize("dim,n_it,N", [(3, 30000, 64), (1, 5000, 16), (5, 20000, 128),
-                                        (2, 999, 2)])
+                                        (2, 999, 2), (8, 60000, 1024), (12, 30000, 100),
+                                        (16, 40000, 37)])
 def test_fill_fp64_matches_oracle(ctx, dim, n_it, N):
     with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=5) as r:
         r.step(L.STAGE_FILL)
@@ -175,8 +176,10 @@ def test_realloc_fp32_form_against_fp64_oracle(ctx):
     assert nh.sum() <= o.sz.n_eval_it + 2 * o.sz.n_cubes
 
 
-def test_refine_matches_oracle(ctx):
-    dim, N = 4, 256
+@pytest.mark.parametrize("dim,N", [(4, 256), (1, 2), (2, 3), (3, 100), (2, 1000), (1, 4096)])
+def test_refine_matches_oracle(ctx, dim, N):
+    """Grid refinement (8-CTA clusters per dimension) against the oracle for
+    bin counts that do and do not divide among the cluster's CTAs."""
     rng = np.random.default_rng(4)
     w = rng.gamma(1.5, 2.0, size=(dim, N))
     c = rng.integers(0, 40, size=(dim, N))
