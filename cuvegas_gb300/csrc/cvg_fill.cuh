@@ -352,7 +352,7 @@ struct cvg_fill_smem {
 template <typename T>
 struct cvg_fill_ctx {
     const T *G;
-    cvg_u32 it, k0, k1, c3;
+    cvg_u32 it, c3;
     int ns, N, kx;
     T dy, fN, fNm1, vc, jac0;
 };
@@ -372,8 +372,6 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
         for (int i = tid; i < D * (N + 1); i += BS) sm.E[i] = grid[i];
     cx.G = ESM ? sm.E : grid;
     cx.it = *a.iteration;
-    cx.k0 = (cvg_u32)a.seed;
-    cx.k1 = (cvg_u32)(a.seed >> 32);
     cx.c3 = a.instance << 8;
     cx.ns = a.n_strat;
     cx.N = N;
