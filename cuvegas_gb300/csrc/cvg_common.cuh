@@ -18,6 +18,7 @@ typedef long long cvg_i64;
 // Status bits written by kernels into the run's status word.
 #define CVG_KSTAT_BAD_TILE 1u      // tile map inconsistent with nh_sum
 #define CVG_KSTAT_NONFINITE 2u     // a non-finite per-cube estimate was seen
+#define CVG_KSTAT_TIMEOUT 4u       // a bounded wait ran out (the results are not valid)
 
 // Philox4x32-10 key schedule of one seed: round r uses (k0 + r*0x9E3779B9,
 // k1 + r*0xBB67AE85).  Kept in the kernel arguments (constant bank), so the

@@ -110,6 +110,8 @@ struct cvg_run_s {
     double *scale_ss = nullptr;
     int *bin_exp = nullptr;
     cvg_u32 *hist_state = nullptr;
+    cvg_u64 *lb = nullptr;        // look-back words of the one-pass allocation
+    cvg_u32 *lb_ctl = nullptr;
     cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
@@ -424,6 +426,8 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.dim = r->f->dim;
     a.rare_shift = 10;    // fixed point while rare updates stay below 1 in 1024
     a.hist_min_it = 2;    // float bin sums in the fill after the first reallocation
+    a.lb = r->lb;
+    a.lb_ctl = r->lb_ctl;
     return a;
 }
 
@@ -573,6 +577,8 @@ cvg_status check_status(cvg_run_s *r)
     CK(cudaStreamSynchronize(r->ctx->stream));
     if (st & CVG_KSTAT_BAD_TILE)
         return fail(CVG_ERR_KERNEL, "fill kernel found an inconsistent tile map");
+    if (st & CVG_KSTAT_TIMEOUT)
+        return fail(CVG_ERR_KERNEL, "the reallocation's look-back wait ran out; results are not valid");
     return CVG_OK;
 }
 
@@ -911,6 +917,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->scale_ss, sizeof(double)},
         {(void **)&r->bin_exp, sizeof(int) * ((size_t)D * N + 1)},
         {(void **)&r->hist_state, 2 * sizeof(cvg_u32)},
+        {(void **)&r->lb, sizeof(cvg_u64) * r->nb},
+        {(void **)&r->lb_ctl, 2 * sizeof(cvg_u32)},
         {(void **)&r->done, 2 * sizeof(cvg_u32)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
@@ -952,6 +960,8 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->iteration, 0, sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->status, 0, sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->done, 0, 2 * sizeof(cvg_u32), st));
+    CK(cudaMemsetAsync(r->lb, 0, sizeof(cvg_u64) * r->nb, st));
+    CK(cudaMemsetAsync(r->lb_ctl, 0, 2 * sizeof(cvg_u32), st));
     {   // the first fill uses fixed-point bin sums with the pilot's exponent table
         const cvg_u32 hs[2] = {1u, 0u};
         CK(cudaMemcpyAsync(r->hist_state, hs, sizeof(hs), cudaMemcpyHostToDevice, st));

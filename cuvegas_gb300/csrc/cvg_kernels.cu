@@ -484,6 +484,145 @@ __device__ __forceinline__ void k3_apply_dev(const cvg_realloc_args &a, unsigned
 
 __global__ void __launch_bounds__(RB) k3_apply(cvg_realloc_args a, unsigned nb) { k3_apply_dev(a, nb, blockIdx.x); }
 
+// ---------------------------------------------------------------------------
+// One-pass allocation (count + scan + apply): each block computes n_h for its
+// chunk of hypercubes, publishes the chunk's sum, and finds the sum of all
+// chunks before it by decoupled look-back over the blocks' published words;
+// then it writes the exclusive prefixes (nh_sum) and the tile map.  Blocks
+// take chunk indices in the order they start (a ticket), so every block a
+// block waits on has started before it; the waits are bounded anyway (a
+// timeout sets CVG_KSTAT_TIMEOUT).  A look-back word packs the launch epoch
+// (bits 34..63), a flag (1 = chunk sum, 2 = inclusive prefix) and a 32-bit
+// value, so the words need no clearing between launches.
+// ---------------------------------------------------------------------------
+constexpr cvg_u64 LB_AGG = 1ull << 32, LB_PRE = 2ull << 32;
+constexpr int LB_SPIN_LIMIT = 1 << 22;
+
+__device__ __forceinline__ cvg_u64 lb_word(cvg_u32 epoch, cvg_u64 flag, cvg_u64 value)
+{
+    return ((cvg_u64)epoch << 34) | flag | (value & 0xFFFFFFFFull);
+}
+// Epochs run 1 .. 2^30 - 1 (0 marks a word never written).
+__device__ __forceinline__ cvg_u32 lb_next_epoch(cvg_u32 e) { return e % 0x3FFFFFFFu + 1u; }
+
+template <int MODE>
+__global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
+{
+    __shared__ cvg_u32 sh[CVG_REALLOC_CHUNK];
+    __shared__ cvg_u64 st[CVG_REALLOC_CHUNK];
+    __shared__ cvg_u64 scratch[33];
+    __shared__ cvg_u64 wtot[RB / 32];
+    __shared__ unsigned s_blk;
+    __shared__ cvg_u32 s_epoch;
+    __shared__ cvg_u64 s_excl;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_epoch = lb_next_epoch(*(volatile cvg_u32 *)&a.lb_ctl[1]);   // read before the ticket
+        __threadfence();
+        s_blk = atomicAdd(&a.lb_ctl[0], 1u);
+    }
+    __syncthreads();
+    const unsigned blk = s_blk;
+    const cvg_u32 epoch = s_epoch;
+    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
+    const cvg_u32 cnt = min((cvg_u32)CVG_REALLOC_CHUNK, a.n_cubes - base);
+
+    // n_h of this chunk (as k3_count)
+    double dsum = 0.0, n_it = 0.0;
+    float scale = 0.f;
+    if (MODE == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
+    if (MODE == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;
+    const float *dh32 = reinterpret_cast<const float *>(a.dh);
+#pragma unroll
+    for (int k = 0; k < RIPT; ++k) {
+        const int i = k * RB + tid;
+        const cvg_u32 c = base + i;
+        cvg_u32 nh = 0u;
+        if ((cvg_u32)i < cnt) {
+            if (MODE == 0) {
+                const double x = a.dh[c] / dsum * n_it;
+                int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
+                nh = ns < 2 ? 2u : (cvg_u32)ns;
+            } else if (MODE == 2) {
+                const float x = dh32[c] * scale;
+                const int ns = (x >= 0.f && x < 2147483520.f) ? (int)x : (x >= 2147483520.f ? 2147483520 : 0);
+                nh = ns < 2 ? 2u : (cvg_u32)ns;
+            } else {
+                nh = a.nh_new[c];
+            }
+        }
+        sh[i] = nh;
+    }
+    __syncthreads();
+    cvg_u64 local = 0;
+#pragma unroll
+    for (int k = 0; k < RIPT; ++k) local += sh[tid * RIPT + k];
+    cvg_u64 off = local;
+    const cvg_u64 agg = block_exscan_u64(off, scratch);
+
+    // decoupled look-back by warp 0, 32 predecessors at a time
+    if (warp == 0) {
+        cvg_u64 excl = 0;
+        bool timeout = false;
+        if (blk == 0) {
+            if (lane == 0) atomicExch((unsigned long long *)&a.lb[0], lb_word(epoch, LB_PRE, agg));
+        } else {
+            if (lane == 0) atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_AGG, agg));
+            int j = (int)blk - 1;
+            while (true) {
+                const int idx = j - lane;
+                cvg_u64 w = 0;
+                int spins = 0;
+                bool ready;
+                do {
+                    w = idx >= 0 ? *(volatile cvg_u64 *)&a.lb[idx] : lb_word(epoch, LB_PRE, 0);
+                    ready = (cvg_u32)(w >> 34) == epoch;
+                } while (!__all_sync(0xffffffffu, ready) && ++spins < LB_SPIN_LIMIT);
+                if (spins >= LB_SPIN_LIMIT) { timeout = true; break; }
+                const unsigned pm = __ballot_sync(0xffffffffu, (w & LB_PRE) != 0);
+                const int lp = pm ? __ffs(pm) - 1 : 31;
+                cvg_u64 v = lane <= lp ? (w & 0xFFFFFFFFull) : 0ull;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                excl += v;
+                if (pm) break;
+                j -= 32;
+            }
+            if (lane == 0) {
+                if (timeout) atomicOr(a.status, CVG_KSTAT_TIMEOUT);
+                atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_PRE, excl + agg));
+            }
+        }
+        if (lane == 0) s_excl = excl;
+    }
+    __syncthreads();
+    off += s_excl;
+
+    // prefixes and tile map (as k3_apply)
+    const cvg_u64 TS = (cvg_u64)a.tile_samples;
+#pragma unroll 1
+    for (int k = 0; k < RIPT; ++k) {
+        const int i = tid * RIPT + k;
+        const cvg_u64 n = sh[i];
+        st[i] = off;
+        if ((cvg_u32)i < cnt) {
+            const cvg_u32 c = base + i;
+            for (cvg_u64 t = (off + TS - 1) / TS; t * TS < off + n && t < a.max_tiles; ++t)
+                a.tile_cube[t] = c;
+        }
+        off += n;
+    }
+    __syncthreads();
+    for (int i = tid; i < (int)cnt; i += RB) a.nh_sum[base + i] = st[i];
+    if (blk == nb - 1 && tid == 0) {
+        // every block has taken its ticket: reset it; the next launch's epoch
+        a.nh_sum[a.n_cubes] = s_excl + agg;
+        a.lb_ctl[0] = 0u;
+        a.lb_ctl[1] = epoch;
+    }
+    (void)wtot;
+}
+
 
 // ---------------------------------------------------------------------------
 // K4: grid refinement, FP64.  One thread-block cluster of CL CTAs per
@@ -971,8 +1110,13 @@ cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s)
     if (a.fast_pow) k3_results_f32<<<nb, RB, 0, s>>>(a);   // + finish in the last block
     else k3_results<<<nb, RB, 0, s>>>(a);
     if (a.adapt) {
-        k3_count<<<nb, RB, 0, s>>>(a, a.fast_pow ? 2 : 0);    // + scan in the last block
-        k3_apply<<<nb, RB, 0, s>>>(a, nb);
+        if (a.lb) {   // one pass: count, scan and apply
+            if (a.fast_pow) k3_alloc<2><<<nb, RB, 0, s>>>(a, nb);
+            else k3_alloc<0><<<nb, RB, 0, s>>>(a, nb);
+        } else {
+            k3_count<<<nb, RB, 0, s>>>(a, a.fast_pow ? 2 : 0);    // + scan in the last block
+            k3_apply<<<nb, RB, 0, s>>>(a, nb);
+        }
     }
     return cudaGetLastError();
 }
@@ -985,8 +1129,12 @@ cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cuda
                                         cudaMemcpyDefault, s);
         if (e != cudaSuccess) return e;
     }
-    k3_count<<<nb, RB, 0, s>>>(a, 1);
-    k3_apply<<<nb, RB, 0, s>>>(a, nb);
+    if (a.lb) {
+        k3_alloc<1><<<nb, RB, 0, s>>>(a, nb);
+    } else {
+        k3_count<<<nb, RB, 0, s>>>(a, 1);
+        k3_apply<<<nb, RB, 0, s>>>(a, nb);
+    }
     return cudaGetLastError();
 }
 

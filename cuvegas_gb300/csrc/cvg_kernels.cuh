@@ -53,6 +53,9 @@ struct cvg_realloc_args {
     int dim;
     int rare_shift;         // fixed point stays while rare updates <= dim*samples / 2^rare_shift
     int hist_min_it;        // first iteration that may use fixed point again after iteration 0
+    cvg_u64 *lb;            // [n_blocks] look-back words of the one-pass allocation, or null
+                            // (three-kernel path); zero before the first launch
+    cvg_u32 *lb_ctl;        // [2]: block ticket (zero between launches), launch epoch
 };
 
 struct cvg_refine_args {
