@@ -50,7 +50,7 @@ SFU_PER_EVAL = DIM                     # one exp per dimension
 PHILOX_PER_EVAL = (DIM + 3) // 4       # Philox4x32-10 calls per evaluation (4 uniforms per call)
 METRIC = "integrand evals/s, VEGAS+ Gaussian d=8, 1e8 evals/iteration (FP32-compensated form)"
 WORKLOAD = "gauss-d8-1e8x20-fp32kahan"
-LAUNCHES_PER_IT = 5                    # fill, 3 reallocation kernels (finish and scan are their tails), refinement
+LAUNCHES_PER_IT = 4                    # fill, 2 reallocation kernels (results+finish, one-pass allocation), refinement
 
 
 def _dist():
