@@ -13,6 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF = os.environ.get("CVG_REFERENCE", "/root/reference")
 DIMS = (2, 3, 4)
+# the reference's kernels for the benchmark workloads' Gaussian (width 0.1),
+# timed on the GPU by tests/golden/time_reference.py
+TIMING = ((4, "0.1"), (8, "0.1"))
 
 
 def build(force=False):
@@ -30,6 +33,16 @@ def build(force=False):
             continue
         cmd = ["nvcc", "-ptx", "-arch=sm_103a", "-O3", "-include", shim, "-DCVG_REF_DIM=%d" % d,
                "-Xcompiler", "-fopenmp", src, "-o", out]
+        subprocess.run(cmd, check=True, capture_output=True, text=True)
+        outs.append(out)
+    for d, width in TIMING:
+        out = os.path.join(OUT, "ref_main_d%d_w%s.ptx" % (d, width.replace(".", "")))
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+                os.path.getmtime(shim), os.path.getmtime(__file__)):
+            outs.append(out)
+            continue
+        cmd = ["nvcc", "-ptx", "-arch=sm_103a", "-O3", "-include", shim, "-DCVG_REF_DIM=%d" % d,
+               "-DCVG_REF_WIDTH=%s" % width, "-Xcompiler", "-fopenmp", src, "-o", out]
         subprocess.run(cmd, check=True, capture_output=True, text=True)
         outs.append(out)
     return outs

@@ -20,13 +20,17 @@ const int blockSizeFill = 64;
 const int blockSizeIntervals = 128;
 const int blockSizeInit = 128;
 const int n_dim = CVG_REF_DIM;
-/* prod_d exp(-((x_d-0.5)/0.2)^2) / (0.2 sqrt(pi)) */
+/* prod_d exp(-((x_d-0.5)/s)^2) / (s sqrt(pi)), s = CVG_REF_WIDTH (0.2 for the
+ * golden vectors, 0.1 for the benchmark workloads) */
+#ifndef CVG_REF_WIDTH
+#define CVG_REF_WIDTH 0.2
+#endif
 __host__ __device__ double integrand(double *x)
 {
     double f = 1.0;
     for (int d = 0; d < n_dim; d++) {
-        double t = (x[d] - 0.5) / 0.2;
-        f *= exp(-t * t) * (1.0 / (0.2 * 1.7724538509055160273));
+        double t = (x[d] - 0.5) / CVG_REF_WIDTH;
+        f *= exp(-t * t) * (1.0 / (CVG_REF_WIDTH * 1.7724538509055160273));
     }
     return f;
 }

@@ -11,7 +11,9 @@
 // sequence as vegasFill (src/main.cu:28-46) on a copy of the generator states
 // taken just before the fill -- curand is called, not re-implemented.
 //
-// Usage: ref_harness <ptx> <dim> <n_eval_it> <n_intervals> <iters> <out_dir>
+// Usage: ref_harness <ptx> <dim> <n_eval_it> <n_intervals> <iters> <out_dir> [time]
+// With "time" nothing is dumped: each iteration (the reference's whole
+// sequence, its host reads included) is timed with CUDA events and printed.
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
@@ -90,6 +92,7 @@ int main(int argc, char **argv)
     int n_intervals = std::atoi(argv[4]);
     const int iters = std::atoi(argv[5]);
     g_out = argv[6];
+    const bool timing = argc > 7 && std::strcmp(argv[7], "time") == 0;
     double alpha = 0.5, beta = 0.75;
     const long max_batch_size = 1048576;
 
@@ -162,7 +165,11 @@ int main(int argc, char **argv)
     CK(cudaMemset(hit, 0, sizeof(bool)));
     CK(cudaMalloc(&states, sizeof(curandState) * batch_size));
     CK(cudaMalloc(&states_copy, sizeof(curandState) * batch_size));
-    CK(cudaMalloc(&ubuf, sizeof(float) * max_eval_it * n_dim));
+    ubuf = nullptr;
+    if (!timing) CK(cudaMalloc(&ubuf, sizeof(float) * max_eval_it * n_dim));
+    cudaEvent_t ev0, ev1;
+    CK(cudaEventCreate(&ev0));
+    CK(cudaEventCreate(&ev1));
 
     // initial grid and nh: src/main.cu:432-448
     std::vector<double> hx(n_dim * n_edges), hdx(n_dim * n_intervals);
@@ -196,13 +203,14 @@ int main(int argc, char **argv)
     CK(cudaMalloc(&t_scan, b_scan));
     CK(cudaMalloc(&t_ex, b_ex));
 
-    FILE *meta = std::fopen((g_out + "/meta.txt").c_str(), "w");
+    FILE *meta = std::fopen((g_out + (timing ? "/meta_time.txt" : "/meta.txt")).c_str(), "w");
     std::fprintf(meta, "dim %d\nn_eval_it %ld\nn_intervals %d\niters %d\nn_strat %d\nn_cubes %d\n"
                        "v_cubes %.17g\nbatch_size %ld\nalpha %.17g\nbeta %.17g\n",
                  n_dim, n_eval_it, n_intervals, iters, n_strat, n_cubes, v_cubes, batch_size,
                  alpha, beta);
 
     for (int it = 0; it < iters; it++) {
+        CK(cudaEventRecord(ev0, 0));
         {   // reset (src/main.cu:525-529)
             void *a1[] = {&n_cubes, &JF, &JF2};
             launch(k_resets, n_cubes, 64, a1);
@@ -219,25 +227,30 @@ int main(int argc, char **argv)
         CK(cudaMemcpy(&last_nh, nh + n_cubes - 1, sizeof(long), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(&last_sum, nh_sum + n_cubes - 1, sizeof(long), cudaMemcpyDeviceToHost));
         long idx = last_sum + last_nh;
-        dump("nh", it, nh, n_cubes);
-        dump("x_edges_in", it, x_edges, (size_t)n_dim * n_edges);
+        if (!timing) {
+            dump("nh", it, nh, n_cubes);
+            dump("x_edges_in", it, x_edges, (size_t)n_dim * n_edges);
+        }
         // fill (src/main.cu:618-628)
         int runs = idx / batch_size + (int)((idx % batch_size) != 0);
-        CK(cudaMemcpy(states_copy, states, sizeof(curandState) * batch_size, cudaMemcpyDeviceToDevice));
+        if (!timing)
+            CK(cudaMemcpy(states_copy, states, sizeof(curandState) * batch_size, cudaMemcpyDeviceToDevice));
         {
             void *a[] = {&n_strat, &n_intervals, &n_edges, &idx, &batch_size, &runs, &counts,
                          &weights, &x_edges, &dx_edges, &JF, &JF2, &evals, &states};
             launch(k_fill, batch_size, 64, a);
         }
-        dump_uniforms<<<(unsigned)((batch_size + 127) / 128), 128>>>(states_copy, n_dim, idx,
-                                                                   batch_size, runs, ubuf);
-        CK(cudaGetLastError());
-        CK(cudaDeviceSynchronize());
-        dump("u", it, ubuf, (size_t)idx * n_dim);
-        dump("JF", it, JF, n_cubes);
-        dump("JF2", it, JF2, n_cubes);
-        dump("weights", it, weights, (size_t)n_dim * n_intervals);
-        dump("counts", it, counts, (size_t)n_dim * n_intervals);
+        if (!timing) {
+            dump_uniforms<<<(unsigned)((batch_size + 127) / 128), 128>>>(states_copy, n_dim, idx,
+                                                                       batch_size, runs, ubuf);
+            CK(cudaGetLastError());
+            CK(cudaDeviceSynchronize());
+            dump("u", it, ubuf, (size_t)idx * n_dim);
+            dump("JF", it, JF, n_cubes);
+            dump("JF2", it, JF2, n_cubes);
+            dump("weights", it, weights, (size_t)n_dim * n_intervals);
+            dump("counts", it, counts, (size_t)n_dim * n_intervals);
+        }
         // remaining (src/main.cu:662-694), serialised on one stream
         {
             void *a[] = {&n_cubes, &v_cubes, &beta, &nh, &JF, &JF2, &dh, &sum_r, &sum_s};
@@ -280,13 +293,22 @@ int main(int argc, char **argv)
             void *a[] = {&n_dim, &n_intervals, &n_edges, &x_edges, &dx_edges};
             launch(k_updx, (long)n_dim * n_intervals, 128, a);
         }
+        CK(cudaEventRecord(ev1, 0));
         CK(cudaDeviceSynchronize());
-        dump("dh", it, dh, n_cubes);
-        dump("nh_next", it, nh, n_cubes);
-        dump("x_edges_out", it, x_edges, (size_t)n_dim * n_edges);
-        dump("res", it, res_s, 1);
-        dump("sig", it, sig_s, 1);
-        dump("dh_sum", it, dh_sum, 1);
+        if (timing) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev0, ev1));
+            double r = 0.0;
+            CK(cudaMemcpy(&r, res_s, sizeof(double), cudaMemcpyDeviceToHost));
+            std::printf("iteration %d samples %ld ms %.4f estimate %.9f\n", it, idx, ms, r);
+        } else {
+            dump("dh", it, dh, n_cubes);
+            dump("nh_next", it, nh, n_cubes);
+            dump("x_edges_out", it, x_edges, (size_t)n_dim * n_edges);
+            dump("res", it, res_s, 1);
+            dump("sig", it, sig_s, 1);
+            dump("dh_sum", it, dh_sum, 1);
+        }
         std::fprintf(meta, "samples_%d %ld\n", it, idx);
     }
     std::fclose(meta);
