@@ -154,6 +154,52 @@ template <> CVG_D double cvg_uniform<double>(cvg_u32 r)
     return __hiloint2double((int)(0x3FF00000u | (r >> 12)), (int)(r << 20)) -
            0.99999999988358467817;  // 1 - 2^-33
 }
+
+// Packed FP32 pairs (PTX .f32x2, sm_100 and later): one instruction applies
+// the same IEEE operation, with the same rounding, to two floats, so two
+// dimensions of the FP32 map issue as one instruction stream.  Each half of
+// a result equals the scalar operation's result.
+typedef unsigned long long cvg_f32x2;
+CVG_D cvg_f32x2 cvg_pack2(float lo, float hi)
+{
+    cvg_f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+CVG_D void cvg_unpack2(cvg_f32x2 r, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+CVG_D cvg_f32x2 cvg_fma2(cvg_f32x2 a, cvg_f32x2 b, cvg_f32x2 c)
+{
+    cvg_f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+CVG_D cvg_f32x2 cvg_add2_rd(cvg_f32x2 a, cvg_f32x2 b)
+{
+    cvg_f32x2 d;
+    asm("add.rm.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CVG_D cvg_f32x2 cvg_add2(cvg_f32x2 a, cvg_f32x2 b)
+{
+    cvg_f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CVG_D cvg_f32x2 cvg_sub2(cvg_f32x2 a, cvg_f32x2 b)
+{
+    cvg_f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CVG_D cvg_f32x2 cvg_mul2(cvg_f32x2 a, cvg_f32x2 b)
+{
+    cvg_f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 #endif  // device
 
 #endif  // CVG_COMMON_CUH

@@ -106,13 +106,52 @@ CVG_D int cvg_bin(float z, int N, float fNm1, float &frac)
     frac = z - bf;
     return __float_as_int(bf + C) - 0x4B000000;
 }
-// Same for z known to be positive (Philox samples): no lower clamp.
+// Same for z known to be positive (Philox samples): no lower clamp.  The
+// clamp is taken on C + floor(z) against C + N - 1 (both exact), whose bits
+// are also the bin index.
 CVG_D int cvg_bin_pos(float z, float fNm1, float &frac)
 {
     const float C = 8388608.0f;
-    const float bf = fminf(__fadd_rd(z, C) - C, fNm1);
-    frac = z - bf;
-    return __float_as_int(bf + C) - 0x4B000000;
+    const float cb = fminf(__fadd_rd(z, C), C + fNm1);
+    frac = z - (cb - C);
+    return __float_as_int(cb) - 0x4B000000;
+}
+
+// FP32 map of one dimension from a Philox word r (src/main.cu:43-52, z = y*N
+// formed from the uniform's significand t: z = t*zs + czs): bin b, mapped x
+// and the Jacobian factor N*dx.  Gd is the dimension's edge table.
+CVG_D void cvg_map_t(cvg_u32 r, float zs, float czs, float fN, float fNm1, const float *Gd,
+                     float &x, int &b, float &jd)
+{
+    float frac;
+    const float z = fmaf(cvg_uniform_t(r), zs, czs);
+    b = cvg_bin_pos(z, fNm1, frac);
+    const float e0 = Gd[b];
+    const float dx = Gd[b + 1] - e0;
+    x = fmaf(dx, frac, e0);
+    jd = fN * dx;
+}
+// The same for two dimensions (Philox words ra, rb; edge tables Ga, Gb) in
+// packed pairs: every result is bit-identical to two cvg_map_t calls.
+CVG_D void cvg_map_t2(cvg_u32 ra, cvg_u32 rb, cvg_f32x2 zs2, cvg_f32x2 czs2, cvg_f32x2 fN2,
+                      float fNm1, const float *Ga, const float *Gb, float &xa, float &xb,
+                      int &ba, int &bb, float &ja, float &jb)
+{
+    const float C = 8388608.0f;
+    const cvg_f32x2 C2 = cvg_pack2(C, C);
+    const cvg_f32x2 z = cvg_fma2(cvg_pack2(cvg_uniform_t(ra), cvg_uniform_t(rb)), zs2, czs2);
+    float ca, cb;
+    cvg_unpack2(cvg_add2_rd(z, C2), ca, cb);
+    ca = fminf(ca, C + fNm1);
+    cb = fminf(cb, C + fNm1);
+    const cvg_f32x2 frac = cvg_sub2(z, cvg_sub2(cvg_pack2(ca, cb), C2));
+    ba = __float_as_int(ca) - 0x4B000000;
+    bb = __float_as_int(cb) - 0x4B000000;
+    const float e0a = Ga[ba], e0b = Gb[bb];
+    const cvg_f32x2 e0 = cvg_pack2(e0a, e0b);
+    const cvg_f32x2 dx = cvg_sub2(cvg_pack2(Ga[ba + 1], Gb[bb + 1]), e0);
+    cvg_unpack2(cvg_fma2(dx, frac, e0), xa, xb);
+    cvg_unpack2(cvg_mul2(fN2, dx), ja, jb);
 }
 CVG_D int cvg_bin(double z, int N, double, double &frac)
 {
@@ -137,6 +176,24 @@ CVG_D int cvg_bin(double z, int N, double, double &frac)
 // wraps adds its 2^32 units to the global FP64 sum; a weight at or above
 // 2^(e+7) (or non-finite) goes to the global FP64 sum directly.
 // FP64 form: FP64 atomics, sums in the reference's precision.
+// The FP32 map runs dimension pairs as packed f32x2 instructions
+// (CVG_FILL_PAIRS), and the fixed-point histogram updates go in groups with
+// their scale arithmetic in f32x2 pairs (CVG_HIST_PAIRS).
+#ifndef CVG_FILL_PAIRS
+#define CVG_FILL_PAIRS 1
+#endif
+#ifndef CVG_HIST_PAIRS
+#define CVG_HIST_PAIRS 1
+#endif
+// Histogram updates issued together (even; 0: 2 in 64-register variants, else 4)
+// and their rare-path form (-1: branch per update in 64-register variants,
+// per group otherwise)
+#ifndef CVG_HIST_GROUP
+#define CVG_HIST_GROUP 0
+#endif
+#ifndef CVG_HIST_BRANCHY
+#define CVG_HIST_BRANCHY -1
+#endif
 #define CVG_HIST_CNT_MASK 0x00FFFFFFu
 #define CVG_HIST_MAX_RUN 0x00FFF000u   // samples between flushes (counts < 2^24)
 // Fixed-point bin sums are used by the FP32 form up to this dimension;
@@ -186,10 +243,85 @@ CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
     const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
     return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
 }
+// One fixed-point value update of bin i (exponent e, scaled weight s and
+// s + 2^23 in qf); the same steps as cvg_hist_add<true>.
+CVG_D cvg_u32 cvg_hist_put(float *hw, double *gw, int i, int e, float s, float qf, float w)
+{
+    if (s < 8388608.0f) {
+        const cvg_u32 q = __float_as_uint(qf) - 0x4B000000u;
+        const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
+        if (o + q < o) {
+            atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
+            return 1u;
+        }
+        return 0u;
+    }
+    atomicAdd(gw + i, cvg_f2d(w));
+    return 1u;
+}
+// G updates (G even; bins i[0..G), one weight w): all count atomics first,
+// then the scale arithmetic in pairs, then the value atomics, so that G
+// shared-memory round trips overlap.  Returns the rare updates (branchy) or
+// leaves their codes in rare[] (branchless).
+template <int G, bool BRANCHY>
+CVG_D cvg_u32 cvg_hist_group(float *hw, cvg_u32 *hc, double *gw, const int *i, float w,
+                             cvg_u32 *rare)
+{
+    const float C = 8388608.0f;
+    int e[G];
+    float s[G], q[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) e[k] = (int)atomicAdd(hc + i[k], 1u) >> 24;
+#pragma unroll
+    for (int k = 0; k < G; k += 2) {
+        const cvg_f32x2 s2 = cvg_mul2(cvg_pack2(w, w),
+                                      cvg_pack2(__int_as_float((143 - e[k]) << 23),
+                                                __int_as_float((143 - e[k + 1]) << 23)));
+        cvg_unpack2(s2, s[k], s[k + 1]);
+        cvg_unpack2(cvg_add2(s2, cvg_pack2(C, C)), q[k], q[k + 1]);
+    }
+    cvg_u32 n = 0;
+    if (BRANCHY) {
+#pragma unroll
+        for (int k = 0; k < G; ++k) n += cvg_hist_put(hw, gw, i[k], e[k], s[k], q[k], w);
+    } else {
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            const bool f = s[k] < C;
+            const cvg_u32 u = f ? __float_as_uint(q[k]) - 0x4B000000u : 0u;
+            const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i[k], u);
+            rare[k] = (f ? 0u : 1u) | (o + u < o ? 2u : 0u);
+        }
+    }
+    return n;
+}
 CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, float w)
 {
     if (rare & 1u) atomicAdd(gw + i, cvg_f2d(w));
     if (rare & 2u) atomicAdd(gw + i, __hiloint2double((1039 + ((int)hc[i] >> 24)) << 20, 0));
+}
+// Dimensions d0..d0+G-1 of one sample (bins bin[], weight w) through
+// cvg_hist_group; returns the number of rare updates.
+template <int G, bool BRANCHY>
+CVG_D cvg_u32 cvg_fill_hist_group(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
+                                  const int *bin, float w)
+{
+    int i[G];
+    cvg_u32 rare[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) i[k] = (d0 + k) * N + bin[d0 + k];
+    cvg_u32 n = cvg_hist_group<G, BRANCHY>(hw, hc, gw, i, w, rare);
+    if (!BRANCHY) {
+        cvg_u32 any = 0;
+#pragma unroll
+        for (int k = 0; k < G; ++k) any |= rare[k];
+        if (any) {
+#pragma unroll
+            for (int k = 0; k < G; ++k)
+                if (rare[k]) { cvg_hist_rare(hc, gw, i[k], rare[k], w); ++n; }
+        }
+    }
+    return n;
 }
 template <bool FIX>
 CVG_D cvg_u32 cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
@@ -444,6 +576,9 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
         constexpr bool ZF = sizeof(T) == 4 && !REPLAY;
         const T zs = ZF ? dy * fN : dy;
         const T zsh = ZF ? (T)0.99999994039535522461 * zs : (T)0;
+#if CVG_FILL_PAIRS
+        const cvg_f32x2 zs2 = cvg_pack2((float)zs, (float)zs), fN2 = cvg_pack2((float)fN, (float)fN);
+#endif
         int coord[D];
         T cdy[D];
         cvg_cube_offsets<D, T>(c, (cvg_u32)ns, zs, zsh, coord, cdy);
@@ -490,6 +625,30 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
             for (int bk = 0; bk < NB; ++bk) {   // 4 dimensions per Philox call
                 cvg_u32x4 r4;
                 if (!REPLAY) r4 = cvg_philox_ks(j, c, cx.it, (cvg_u32)bk | cx.c3, keys);
+#if CVG_FILL_PAIRS
+                if constexpr (ZF) {
+                    // dimension pairs in packed FP32 (same results as below)
+                    const float *Gb = reinterpret_cast<const float *>(G);
+#pragma unroll
+                    for (int q = 0; q < 4; q += 2) {
+                        const int d = 4 * bk + q;
+                        if (d >= D) break;
+                        const cvg_u32 ra = q == 0 ? r4.x : r4.z, rb = q == 0 ? r4.y : r4.w;
+                        float ja, jb;
+                        if (d + 1 < D) {
+                            cvg_map_t2(ra, rb, zs2, cvg_pack2(cdy[d], cdy[d + 1]), fN2, fNm1,
+                                       Gb + d * (N + 1), Gb + (d + 1) * (N + 1), x[d], x[d + 1],
+                                       bin[d], bin[d + 1], ja, jb);
+                            jac *= ja;
+                            jac *= jb;
+                        } else {
+                            cvg_map_t(ra, zs, cdy[d], fN, fNm1, Gb + d * (N + 1), x[d], bin[d], ja);
+                            jac *= ja;
+                        }
+                    }
+                    continue;
+                }
+#endif
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     const int d = 4 * bk + q;
@@ -525,7 +684,29 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 const T jf = (T)F::f(x, sm.th) * jac;
                 const T jf2 = jf * jf;
                 if constexpr (H && FIX) {
+#if CVG_HIST_PAIRS
+                    // fixed-point bin sums in groups of dimensions (count
+                    // atomics together, scale arithmetic in f32x2 pairs); a
+                    // wrap or a large weight (rare) is handled behind a
+                    // branch: per update where the kernel is held to 64
+                    // registers (fewer values live), per group otherwise
 #ifdef CVG_FILL_LOWREG
+                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 2;
+                    constexpr bool BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY != 0 : true;
+#else
+                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 4;
+                    constexpr bool BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY != 0 : false;
+#endif
+                    constexpr int R0 = (D / HG) * HG;
+#pragma unroll
+                    for (int d0 = 0; d0 < R0; d0 += HG)
+                        nrare += cvg_fill_hist_group<HG, BR>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                    if constexpr (D - R0 >= 2)
+                        nrare += cvg_fill_hist_group<2, BR>(sm.hw, sm.hc, a.weights, R0, N, bin, jf2);
+                    if constexpr ((D - R0) & 1)
+                        nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights,
+                                                    (D - 1) * N + bin[D - 1], jf2);
+#elif defined(CVG_FILL_LOWREG)
                     // held to 64 registers (2 CTAs per SM): branches keep the
                     // dimensions' updates apart and fewer values live
 #pragma unroll

@@ -82,8 +82,9 @@ static void launch(cudaKernel_t k, long n, int block, void **args)
 
 int main(int argc, char **argv)
 {
-    if (argc != 7) {
-        std::fprintf(stderr, "usage: %s ptx dim n_eval_it n_intervals iters out_dir\n", argv[0]);
+    if (argc != 7 && argc != 8) {
+        std::fprintf(stderr, "usage: %s ptx dim n_eval_it n_intervals iters out_dir [time]\n",
+                     argv[0]);
         return 1;
     }
     const char *ptx_path = argv[1];

@@ -32,7 +32,9 @@ def main(out_dir):
     for name, dim, n_it, nb, iters in CASES:
         ptx = os.path.join(ROOT, "oracle", "_ref", "ref_main_d%d_w01.ptx" % dim)
         r = subprocess.run([exe, ptx, str(dim), str(n_it), str(nb), str(iters), work, "time"],
-                           check=True, capture_output=True, text=True)
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.exit("%s: harness exited %d\n%s%s" % (name, r.returncode, r.stdout, r.stderr))
         rows = [tuple(float(v) for v in re.findall(r"samples (\d+) ms ([\d.]+)", line)[0])
                 for line in r.stdout.splitlines() if line.startswith("iteration")]
         warm = rows[2:] if len(rows) > 3 else rows
