@@ -313,6 +313,6 @@ int main(int argc, char **argv)
         std::fprintf(meta, "samples_%d %ld\n", it, idx);
     }
     std::fclose(meta);
-    std::printf("golden written to %s\n", g_out.c_str());
+    if (!timing) std::printf("golden written to %s\n", g_out.c_str());
     return 0;
 }
