@@ -809,7 +809,9 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
     const int tid = threadIdx.x;
     const int TS = a.tile_samples;
     cvg_fill_smem<D, T, ESM, HSM, P, GRAD> sm;
-    sm.carve(cvg_smem, a.n_intervals, TS);
+    // bins fixed at compile time: the views sit at constant offsets, so one
+    // scaled bin index addresses both histogram words
+    sm.carve(cvg_smem, NI > 0 ? NI : a.n_intervals, TS);
     cvg_fill_ctx<T> cx;
     cvg_fill_setup<D, T, BS, ESM, HSM, P, GRAD, FIX>(a, sm, cx);
     cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
