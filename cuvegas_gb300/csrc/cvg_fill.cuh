@@ -185,9 +185,11 @@ CVG_D int cvg_bin(double z, int N, double, double &frac)
 #ifndef CVG_HIST_PAIRS
 #define CVG_HIST_PAIRS 1
 #endif
-// Histogram updates issued together (even; 0: 2 in 64-register variants, else 4)
-// and their rare-path form (-1: branch per update in 64-register variants,
-// per group otherwise)
+// Histogram updates issued together (even; 0: 8) and their rare-path form
+// (1: a branch per update, 0: per group, 2 or -1: per sample).  Measured on
+// GB300 (fill ms, d=8 Gaussian 1e8 / d=16 corner 1e9): per update in pairs
+// 1.898 / -, per group of 4 - / 30.95, per sample in groups of 4
+// 1.875 / 30.52, of 8 1.869 / 29.57, of 16 - / 29.92.
 #ifndef CVG_HIST_GROUP
 #define CVG_HIST_GROUP 0
 #endif
@@ -302,6 +304,22 @@ CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, flo
 }
 // Dimensions d0..d0+G-1 of one sample (bins bin[], weight w) through
 // cvg_hist_group; returns the number of rare updates.
+// The same with the rare codes of the group returned as 2-bit fields at
+// bit 2*(d0+k) of a per-sample mask (handled once per sample).
+template <int G>
+CVG_D cvg_u32 cvg_fill_hist_group_mask(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
+                                       const int *bin, float w)
+{
+    int i[G];
+    cvg_u32 rare[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) i[k] = (d0 + k) * N + bin[d0 + k];
+    cvg_hist_group<G, false>(hw, hc, gw, i, w, rare);
+    cvg_u32 m = 0;
+#pragma unroll
+    for (int k = 0; k < G; ++k) m |= rare[k] << (2 * (d0 + k));
+    return m;
+}
 template <int G, bool BRANCHY>
 CVG_D cvg_u32 cvg_fill_hist_group(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
                                   const int *bin, float w)
@@ -425,31 +443,59 @@ CVG_D void cvg_run_to_global(const cvg_fill_args &a, cvg_u32 c, const cvg_acc<do
     atomicAdd(&a.JF2[c], v2);
 }
 
+// Digits of the current cube in base n_strat.  With D >= 4 every digit is
+// below 256 (n_strat^D < 2^32 hypercubes), so four share a register.
+template <int D, bool PACK = (D >= 4)>
+struct cvg_coords {
+    int v[D];
+    CVG_D void clear() {}
+    CVG_D int get(int d) const { return v[d]; }
+    CVG_D void set(int d, int x) { v[d] = x; }
+};
+template <int D>
+struct cvg_coords<D, true> {
+    cvg_u32 w[(D + 3) / 4];
+    CVG_D void clear()
+    {
+#pragma unroll
+        for (int k = 0; k < (D + 3) / 4; ++k) w[k] = 0u;
+    }
+    CVG_D int get(int d) const { return (int)((w[d >> 2] >> (8 * (d & 3))) & 0xFFu); }
+    CVG_D void set(int d, int x)
+    {
+        const int sh = 8 * (d & 3);
+        w[d >> 2] = (w[d >> 2] & ~(0xFFu << sh)) | ((cvg_u32)x << sh);
+    }
+};
+
 // Stratum offsets coord_d * dy - sh of cube c (digit d of c in base n_strat,
 // least significant first: src/main.cu:43-47); cvg_cube_next steps to cube
 // c+1 like an odometer.  sh = 0 gives the reference's coord * dy.
 template <int D, typename T>
-CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, T sh, int *coord, T *cdy)
+CVG_D void cvg_cube_offsets(cvg_u32 c, cvg_u32 ns, T dy, T sh, cvg_coords<D> &co, T *cdy)
 {
+    co.clear();
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const cvg_u32 q = c / ns;
-        coord[d] = (int)(c - q * ns);
-        cdy[d] = (T)coord[d] * dy - sh;
+        const int v = (int)(c - q * ns);
+        co.set(d, v);
+        cdy[d] = (T)v * dy - sh;
         c = q;
     }
 }
 template <int D, typename T>
-CVG_D void cvg_cube_next(int ns, T dy, T sh, int *coord, T *cdy)
+CVG_D void cvg_cube_next(int ns, T dy, T sh, cvg_coords<D> &co, T *cdy)
 {
     bool carry = true;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         if (carry) {
-            const int v = coord[d] + 1;
+            const int v = co.get(d) + 1;
             carry = v == ns;
-            coord[d] = carry ? 0 : v;
-            cdy[d] = (T)coord[d] * dy - sh;
+            const int nv = carry ? 0 : v;
+            co.set(d, nv);
+            cdy[d] = (T)nv * dy - sh;
         }
     }
 }
@@ -579,7 +625,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
 #if CVG_FILL_PAIRS
         const cvg_f32x2 zs2 = cvg_pack2((float)zs, (float)zs), fN2 = cvg_pack2((float)fN, (float)fN);
 #endif
-        int coord[D];
+        cvg_coords<D> coord;
         T cdy[D];
         cvg_cube_offsets<D, T>(c, (cvg_u32)ns, zs, zsh, coord, cdy);
         const int lend = min(l0 + spt, lend_tile);
@@ -686,26 +732,47 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 if constexpr (H && FIX) {
 #if CVG_HIST_PAIRS
                     // fixed-point bin sums in groups of dimensions (count
-                    // atomics together, scale arithmetic in f32x2 pairs); a
-                    // wrap or a large weight (rare) is handled behind a
-                    // branch: per update where the kernel is held to 64
-                    // registers (fewer values live), per group otherwise
-#ifdef CVG_FILL_LOWREG
-                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 2;
-                    constexpr bool BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY != 0 : true;
-#else
-                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 4;
-                    constexpr bool BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY != 0 : false;
-#endif
+                    // atomics together, scale arithmetic in f32x2 pairs); the
+                    // rare updates (a wrap or a large weight) of all
+                    // dimensions are collected in a mask and handled behind
+                    // one branch per sample
+                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 8;
+                    constexpr int BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY : 2;
+                    // groups of HG, then of 4 and 2, then one dimension
                     constexpr int R0 = (D / HG) * HG;
+                    constexpr int R1 = R0 + ((D - R0) / 4) * 4;
+                    constexpr int R2 = R1 + ((D - R1) / 2) * 2;
+                    if constexpr (BR == 2 && D <= 16) {
+                        cvg_u32 m = 0;
 #pragma unroll
-                    for (int d0 = 0; d0 < R0; d0 += HG)
-                        nrare += cvg_fill_hist_group<HG, BR>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
-                    if constexpr (D - R0 >= 2)
-                        nrare += cvg_fill_hist_group<2, BR>(sm.hw, sm.hc, a.weights, R0, N, bin, jf2);
-                    if constexpr ((D - R0) & 1)
-                        nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights,
-                                                    (D - 1) * N + bin[D - 1], jf2);
+                        for (int d0 = 0; d0 < R0; d0 += HG)
+                            m |= cvg_fill_hist_group_mask<HG>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+#pragma unroll
+                        for (int d0 = R0; d0 < R1; d0 += 4)
+                            m |= cvg_fill_hist_group_mask<4>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                        if constexpr (R2 > R1)
+                            m |= cvg_fill_hist_group_mask<2>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
+                        if constexpr (D > R2)
+                            m |= cvg_hist_add_fix(sm.hw, sm.hc, R2 * N + bin[R2], jf2) << (2 * R2);
+                        if (m) {
+#pragma unroll
+                            for (int d = 0; d < D; ++d) {
+                                const cvg_u32 r = (m >> (2 * d)) & 3u;
+                                if (r) { cvg_hist_rare(sm.hc, a.weights, d * N + bin[d], r, jf2); ++nrare; }
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int d0 = 0; d0 < R0; d0 += HG)
+                            nrare += cvg_fill_hist_group<HG, BR == 1>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+#pragma unroll
+                        for (int d0 = R0; d0 < R1; d0 += 4)
+                            nrare += cvg_fill_hist_group<4, BR == 1>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                        if constexpr (R2 > R1)
+                            nrare += cvg_fill_hist_group<2, BR == 1>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
+                        if constexpr (D > R2)
+                            nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights, R2 * N + bin[R2], jf2);
+                    }
 #elif defined(CVG_FILL_LOWREG)
                     // held to 64 registers (2 CTAs per SM): branches keep the
                     // dimensions' updates apart and fewer values live

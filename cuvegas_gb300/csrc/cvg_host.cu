@@ -962,10 +962,11 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->done, 0, 2 * sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->lb, 0, sizeof(cvg_u64) * r->nb, st));
     CK(cudaMemsetAsync(r->lb_ctl, 0, 2 * sizeof(cvg_u32), st));
-    {   // the first fill uses fixed-point bin sums with the pilot's exponent table
-        const cvg_u32 hs[2] = {1u, 0u};
-        CK(cudaMemcpyAsync(r->hist_state, hs, sizeof(hs), cudaMemcpyHostToDevice, st));
-    }
+    // the first fill keeps float bin sums: the pilot's ~150 samples per bin
+    // cannot bound the mean of a heavy-tailed bin (a d=16 Gaussian lost 2.8 %
+    // of a dimension's sum to fixed point on the pilot's table); fixed point
+    // starts from the third fill, on a table built from a whole fill's sums
+    CK(cudaMemsetAsync(r->hist_state, 0, 2 * sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->stats, 0, sizeof(double) * 3 * p.max_it, st));
     CK(cudaMemsetAsync(r->grad, 0, sizeof(double) * std::max(1, f->n_params), st));
     if (f->n_params > 0)

@@ -22,6 +22,12 @@ def make_run(ctx, src, dim, n_it, max_it, N=64, prec=L.PREC_FP64, seed=1, theta=
     return runtime.Run(f, p, theta)
 
 
+def force_fixed_point(r):
+    """Next fill of an FP32 run with fixed-point bin sums (the first fill of a
+    run keeps float sums; its exponent table is the pilot's)."""
+    r.set(L.BUF_HIST_STATE, np.array([1, 0], dtype=np.uint32))
+
+
 def oracle_run(dim, n_it, max_it, N=64):
     return P.OracleRun(dim, n_it * max_it, max_it, n_intervals=N)
 
@@ -57,6 +63,7 @@ def test_fill_fp32_histograms_against_oracle(ctx):
     dim, n_it, N = 3, 200000, 64
     with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=5, prec=L.PREC_FP32) as r:
         k = int(r.get(L.BUF_SCALE_EXP)[0])
+        force_fixed_point(r)
         r.step(L.STAGE_FILL)
         JF, W, Cn = r.get(L.BUF_JF), r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
     W = W * 4.0 ** k
@@ -70,6 +77,32 @@ def test_fill_fp32_histograms_against_oracle(ctx):
     # are ~1e-20 of the central ones (the refinement's damping weighs them)
     assert o.weights.min() < 1e-15 * o.weights.max()
     np.testing.assert_allclose(W, o.weights, rtol=2e-3, atol=0)
+    np.testing.assert_allclose(JF.sum(), o.JF.sum(), rtol=1e-5)
+
+
+@pytest.mark.parametrize("dim,n_it,N,fixed", [(2, 50000, 64, True), (5, 100000, 64, True),
+                                              (7, 100000, 64, True), (8, 100000, 1024, True),
+                                              (12, 60000, 64, True), (16, 60000, 64, False),
+                                              (8, 100000, 1024, False)])
+def test_fill_fp32_histograms_every_dimension(ctx, dim, n_it, N, fixed):
+    """FP32 form at dimensions whose fixed-point histogram updates split into
+    groups of 8, 4, 2 and 1: every dimension's counts and per-dimension sums
+    against the FP64 oracle on the same Philox words.  The d=16 Gaussian's
+    pilot table is too coarse for fixed point (a bin's pilot mean 2^26 above
+    its fill weights), which is why a run's first fill keeps float sums."""
+    with make_run(ctx, I.GAUSS, dim, n_it, 4, N=N, seed=7, prec=L.PREC_FP32) as r:
+        k = int(r.get(L.BUF_SCALE_EXP)[0])
+        if fixed:
+            force_fixed_point(r)
+        r.step(L.STAGE_FILL)
+        JF, W, Cn = r.get(L.BUF_JF), r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+    W = W * 4.0 ** k
+    o = oracle_run(dim, n_it, 4, N)
+    u, _ = P.uniforms(P.U_PHILOX_F32, seed=7)
+    S = o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    assert np.array_equal(Cn.astype(np.int64).sum(axis=1), np.full(dim, S))
+    assert np.abs(Cn.astype(np.int64) - o.counts).sum() <= 2e-4 * S * dim
+    np.testing.assert_allclose(W.sum(axis=1), o.weights.sum(axis=1), rtol=2e-5)
     np.testing.assert_allclose(JF.sum(), o.JF.sum(), rtol=1e-5)
 
 
@@ -104,6 +137,7 @@ def test_fill_fp32_histogram_word_wraps(ctx):
                   block=1024, spt=64) as r:
         assert int(r.get(L.BUF_SCALE_EXP)[0]) == 0
         assert r.info.block * r.info.spt == 65536
+        force_fixed_point(r)
         r.step(L.STAGE_FILL)
         W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
         r.step(L.STAGE_REALLOC | L.STAGE_REFINE)

@@ -37,7 +37,8 @@ def test_resume_from_checkpoint_equals_one_run(ctx, prec, tmp_path):
     np.testing.assert_allclose(it_res, ref_it, rtol=2e-5)
     np.testing.assert_allclose(edges, ref_edges, rtol=1e-6, atol=1e-8)
     assert abs(res.result - ref.result) <= 2e-5 * abs(ref.result)
-    assert res.tot_nevals == ref.tot_nevals
+    # the same rounding can move a hypercube's n_h = floor(...) by one
+    assert abs(res.tot_nevals - ref.tot_nevals) <= max(8, 1e-5 * ref.tot_nevals)
 
 
 def test_trained_map_without_adaptation(ctx):
