@@ -445,8 +445,26 @@ __device__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb)
     if (threadIdx.x == 0) a.bsums[nb] = total;
 }
 
-
-
+// Prefixes st[] of this thread's RIPT hypercubes (sh[] holds their n_h, off is
+// the first one's prefix) and the tile map: tile t (samples [t*TS, (t+1)*TS))
+// records the hypercube holding its first sample.  One division per thread;
+// the tile index then only advances (t*TS >= off at every hypercube).
+__device__ __forceinline__ void k3_prefix_tiles(const cvg_realloc_args &a, const cvg_u32 *sh,
+                                                cvg_u64 *st, cvg_u64 off, cvg_u32 base, cvg_u32 cnt)
+{
+    const cvg_u64 TS = (cvg_u64)a.tile_samples;
+    cvg_u64 t = (off + TS - 1) / TS;
+    cvg_u64 ts = t * TS;
+#pragma unroll 1
+    for (int k = 0; k < RIPT; ++k) {
+        const int i = threadIdx.x * RIPT + k;
+        const cvg_u64 n = sh[i];
+        st[i] = off;
+        if ((cvg_u32)i < cnt)
+            for (; ts < off + n && t < a.max_tiles; ++t, ts += TS) a.tile_cube[t] = base + i;
+        off += n;
+    }
+}
 
 __device__ __forceinline__ void k3_apply_dev(const cvg_realloc_args &a, unsigned nb, const unsigned blk)
 {
@@ -464,19 +482,7 @@ __device__ __forceinline__ void k3_apply_dev(const cvg_realloc_args &a, unsigned
     cvg_u64 off = local;
     block_exscan_u64(off, scratch);
     off += a.bsums[blk];
-    const cvg_u64 TS = (cvg_u64)a.tile_samples;
-#pragma unroll 1
-    for (int k = 0; k < RIPT; ++k) {
-        const int i = threadIdx.x * RIPT + k;
-        const cvg_u64 n = sh[i];
-        st[i] = off;
-        if ((cvg_u32)i < cnt) {
-            const cvg_u32 c = base + i;
-            for (cvg_u64 t = (off + TS - 1) / TS; t * TS < off + n && t < a.max_tiles; ++t)
-                a.tile_cube[t] = c;
-        }
-        off += n;
-    }
+    k3_prefix_tiles(a, sh, st, off, base, cnt);
     __syncthreads();
     for (int i = threadIdx.x; i < (int)cnt; i += RB) a.nh_sum[base + i] = st[i];
     if (blk == nb - 1 && threadIdx.x == 0) a.nh_sum[a.n_cubes] = a.bsums[nb];
@@ -599,19 +605,7 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
     off += s_excl;
 
     // prefixes and tile map (as k3_apply)
-    const cvg_u64 TS = (cvg_u64)a.tile_samples;
-#pragma unroll 1
-    for (int k = 0; k < RIPT; ++k) {
-        const int i = tid * RIPT + k;
-        const cvg_u64 n = sh[i];
-        st[i] = off;
-        if ((cvg_u32)i < cnt) {
-            const cvg_u32 c = base + i;
-            for (cvg_u64 t = (off + TS - 1) / TS; t * TS < off + n && t < a.max_tiles; ++t)
-                a.tile_cube[t] = c;
-        }
-        off += n;
-    }
+    k3_prefix_tiles(a, sh, st, off, base, cnt);
     __syncthreads();
     for (int i = tid; i < (int)cnt; i += RB) a.nh_sum[base + i] = st[i];
     if (blk == nb - 1 && tid == 0) {
