@@ -48,6 +48,8 @@ struct cvg_fill_args {
     cvg_u32 *counts;              // [dim][N] samples per bin
     double *grad;                 // [n_params] dI/dtheta accumulator (gradient pass)
     cvg_u32 *status;              // error bits
+    cvg_u32 *tile_ctl;            // warp tiles: [0] next tile to claim, [1] CTAs done (zero
+                                  // between launches: the last CTA of a launch resets both)
     int *scale_exp;               // FP32 form: f*jac is scaled by 2^-scale_exp (may be null)
     double *scale_ss;             // FP32-form pilot: sum of (f*jac)^2 over its samples
     cvg_u32 *hist_state;          // FP32 form: [0] 1 = fixed-point bin sums in this fill,
@@ -61,7 +63,7 @@ struct cvg_fill_args {
     cvg_u32 n_cubes;
     int n_strat;
     int n_intervals;
-    int tile_samples;             // samples per tile = blockDim.x * spt
+    int tile_samples;             // samples per tile: 32 * spt (warp tiles) or blockDim.x * spt
     int spt;                      // consecutive samples per thread
     int n_params;
     int pad0;
@@ -80,18 +82,27 @@ struct cvg_batch_args {
 
 CVG_HD cvg_u64 cvg_align16(cvg_u64 x) { return (x + 15ull) & ~15ull; }
 
+// Single-instance fills give each warp its own tiles of 32 * spt samples
+// (no block-wide barrier between tiles; warps claim tiles from a counter);
+// the batched fill keeps block-wide tiles.
+#ifndef CVG_FILL_WARP_TILES
+#define CVG_FILL_WARP_TILES 1
+#endif
+
 // Dynamic shared memory of one fill launch; the kernel carves it in the same
 // order: theta | bin sums | grid | bin counts | cube starts | reduce scratch.
+// groups: tiles in flight per CTA (block / 32 with warp tiles, else 1), each
+// with its own cube-start buffer.
 CVG_HD cvg_u64 cvg_fill_smem_bytes(int dim, int n_intervals, int tsz, int edges_smem,
                                    int hist_smem, int grad, int tile_samples, int n_params,
-                                   int block)
+                                   int block, int groups = 1)
 {
     cvg_u64 b = cvg_align16((cvg_u64)n_params * tsz);
     const int h = hist_smem && !grad;
     if (h) b += cvg_align16((cvg_u64)dim * n_intervals * tsz);
     if (edges_smem) b += cvg_align16((cvg_u64)dim * (n_intervals + 1) * tsz);
     if (h) b += cvg_align16((cvg_u64)dim * n_intervals * 4);
-    b += cvg_align16((cvg_u64)(tile_samples / 2 + 4) * 4);
+    b += cvg_align16((cvg_u64)groups * (tile_samples / 2 + 4) * 4);
     if (grad) b += cvg_align16((cvg_u64)(block / 32) * n_params * 8);
     return b;
 }

@@ -508,7 +508,7 @@ struct cvg_fill_smem {
     cvg_u32 *hc;
     int *starts;
     double *red;
-    CVG_D void carve(unsigned char *base, int N, int TS)
+    CVG_D void carve(unsigned char *base, int N, int TS, int groups = 1)
     {
         constexpr bool H = HSM && !GRAD;
         cvg_u64 off = 0;
@@ -521,7 +521,7 @@ struct cvg_fill_smem {
         hc = (cvg_u32 *)(base + off);
         if (H) off += cvg_align16((cvg_u64)D * N * 4);
         starts = (int *)(base + off);
-        off += cvg_align16((cvg_u64)(TS / 2 + 4) * 4);
+        off += cvg_align16((cvg_u64)groups * (TS / 2 + 4) * 4);
         red = (double *)(base + off);
     }
 };
@@ -573,10 +573,15 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     }
 }
 
-// One tile: samples [tile*TS, min((tile+1)*TS, S)).  Returns false (and sets a
-// status bit) if the tile map is inconsistent; uniform across the block.
+// One tile: samples [tile*TS, min((tile+1)*TS, S)), taken by the whole CTA
+// or (WT) by one warp.  Returns false (and sets a status bit) if the tile map
+// is inconsistent; uniform across the block (warp).
+template <bool WT> CVG_D void cvg_tile_sync()
+{
+    if (WT) __syncwarp(); else __syncthreads();
+}
 template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
-          int NI, bool FIX>
+          int NI, bool FIX, bool WT = false>
 CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, HSM, P, GRAD> &sm,
                          const cvg_fill_ctx<T> &cx, cvg_u64 tile, cvg_u64 n_tiles, cvg_u64 S,
                          cvg_acc<T> *gacc, cvg_u32 &nrare, const cvg_philox_keys &keys)
@@ -584,11 +589,12 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
     constexpr int PP = P > 0 ? P : 1;
     constexpr int NB = (D + 3) / 4;
     constexpr bool H = HSM && !GRAD;
-    const int tid = threadIdx.x;
+    constexpr int GS = WT ? 32 : BS;   // threads sharing the tile
+    const int tid = WT ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
     const int TS = a.tile_samples, N = NI > 0 ? NI : cx.N, ns = cx.ns;   // NI: bins fixed at compile time
     const T dy = cx.dy, fN = cx.fN, fNm1 = cx.fNm1;
     const T *G = cx.G;
-    int *starts = sm.starts;
+    int *starts = sm.starts + (WT ? (int)(threadIdx.x >> 5) * (TS / 2 + 4) : 0);
     const cvg_u64 base = tile * (cvg_u64)TS;
     const cvg_u32 c_lo = a.tile_cube[tile];
     const cvg_u32 c_hi = (tile + 1 < n_tiles) ? a.tile_cube[tile + 1] : a.n_cubes - 1;
@@ -597,9 +603,9 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
         return false;
     }
     const int K = (int)(c_hi - c_lo) + 2;
-    for (int i = tid; i < K; i += BS)
+    for (int i = tid; i < K; i += GS)
         starts[i] = (int)((cvg_i64)a.nh_sum[c_lo + i] - (cvg_i64)base);
-    __syncthreads();
+    cvg_tile_sync<WT>();
 
     const int spt = a.spt;
     const int l0 = tid * spt;
@@ -820,7 +826,7 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
             }
         }
     }
-    __syncthreads();
+    cvg_tile_sync<WT>();
     return true;
 }
 
@@ -865,20 +871,27 @@ CVG_D bool cvg_fill_use_fixed(const cvg_fill_args &a)
     return cvg_hist_fixed<D, T>() && (!a.hist_state || a.hist_state[0] != 0u);
 }
 
-// Persistent single-instance fill: this CTA takes tiles blockIdx.x,
-// blockIdx.x + gridDim.x, ...
+// Persistent single-instance fill.  Block tiles: this CTA takes tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ...  Warp tiles (CVG_FILL_WARP_TILES):
+// each warp claims tiles of 32 * spt samples from a launch-wide counter, one
+// ahead of the tile it works on, with no barrier between tiles, so the warps
+// of a CTA drift into different phases (sampler, map, histogram) and the
+// launch ends within one warp tile of its average.  A CTA claims at most
+// CVG_HIST_MAX_RUN samples (its histogram counts stay below 2^24); the grid's
+// budget (>= 152 CTAs) exceeds the 2^31 samples an iteration may hold.
 template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
           int NI, bool FIX>
 CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
     constexpr int PP = P > 0 ? P : 1;
+    constexpr bool WT = CVG_FILL_WARP_TILES != 0;
     const int tid = threadIdx.x;
     const int TS = a.tile_samples;
     cvg_fill_smem<D, T, ESM, HSM, P, GRAD> sm;
     // bins fixed at compile time: the views sit at constant offsets, so one
     // scaled bin index addresses both histogram words
-    sm.carve(cvg_smem, NI > 0 ? NI : a.n_intervals, TS);
+    sm.carve(cvg_smem, NI > 0 ? NI : a.n_intervals, TS, WT ? BS / 32 : 1);
     cvg_fill_ctx<T> cx;
     cvg_fill_setup<D, T, BS, ESM, HSM, P, GRAD, FIX>(a, sm, cx);
     cvg_acc<T> gacc[PP];   // gradient pass: sum over runs of (v_cubes/nh) * run sum
@@ -887,19 +900,54 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
     __syncthreads();
 
     cvg_u32 nrare = 0;
-    cvg_u64 since = 0;   // samples in the shared histograms since their last flush
-    for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-        if (since + (cvg_u64)TS > CVG_HIST_MAX_RUN) {
-            cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm, true);
-            since = 0;
+    if constexpr (WT) {
+        // tile (warp number) first, then tiles n_warps, n_warps + 1, ... from the
+        // counter (no burst of claims at the start)
+        __shared__ cvg_u32 claimed;   // samples this CTA has claimed
+        constexpr int W = BS / 32;
+        if (tid == 0) claimed = (cvg_u32)(W * TS);
+        __syncthreads();
+        const cvg_u32 lane = tid & 31;
+        const cvg_u64 n_warps = (cvg_u64)gridDim.x * W;
+        auto claim = [&]() -> cvg_u64 {
+            cvg_u32 t = 0xFFFFFFFFu;
+            if (lane == 0 && atomicAdd(&claimed, (cvg_u32)TS) + (cvg_u32)TS <= CVG_HIST_MAX_RUN)
+                t = atomicAdd(&a.tile_ctl[0], 1u);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            return t == 0xFFFFFFFFu ? ~0ull : n_warps + t;
+        };
+        cvg_u64 tile = (cvg_u64)blockIdx.x * W + (tid >> 5);
+        while (tile < n_tiles) {
+            const cvg_u64 next = n_warps < n_tiles ? claim() : ~0ull;
+            if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX, true>(
+                    a, sm, cx, tile, n_tiles, S, gacc, nrare, a.keys))
+                break;
+            tile = next;
         }
-        since += (cvg_u64)TS;
-        if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX>(a, sm, cx, tile, n_tiles,
-                                                                           S, gacc, nrare, a.keys))
-            break;
+    } else {
+        cvg_u64 since = 0;   // samples in the shared histograms since their last flush
+        for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+            if (since + (cvg_u64)TS > CVG_HIST_MAX_RUN) {
+                cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm, true);
+                since = 0;
+            }
+            since += (cvg_u64)TS;
+            if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX>(a, sm, cx, tile,
+                                                                               n_tiles, S, gacc,
+                                                                               nrare, a.keys))
+                break;
+        }
     }
 
     cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm);
+    if (WT && tid == 0) {   // the last CTA resets the tile counter for the next launch
+        __threadfence();
+        if (atomicAdd(&a.tile_ctl[1], 1u) == gridDim.x - 1) {
+            a.tile_ctl[0] = 0u;
+            a.tile_ctl[1] = 0u;
+            __threadfence();
+        }
+    }
     if (FIX) cvg_fill_count_rare(a, nrare);
     if (GRAD) {
         const int lane = tid & 31, warp = tid >> 5;
@@ -930,7 +978,9 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
         n_tiles = a.max_tiles;
     }
-    if ((cvg_u64)blockIdx.x >= n_tiles) return;
+    // with warp tiles every CTA takes part (the last one to finish resets the
+    // tile counter)
+    if (!CVG_FILL_WARP_TILES && (cvg_u64)blockIdx.x >= n_tiles) return;
     if constexpr (cvg_hist_fixed<D, T>() && HSM && !GRAD) {
         if (cvg_fill_use_fixed<D, T>(a))
             cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, true>(a, S, n_tiles);

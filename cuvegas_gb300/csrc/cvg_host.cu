@@ -97,6 +97,7 @@ struct cvg_run_s {
     unsigned nb = 0;
     cvg_u64 max_tiles = 0;
     int block = 0, spt = 0, TS = 0, grid = 0, esm = 1, hsm = 1;
+    int wt = 1;                   // warp tiles (TS = 32*spt) or block tiles (TS = block*spt)
     int it_done = 0;
     // device memory (one arena)
     void *arena = nullptr;
@@ -112,6 +113,7 @@ struct cvg_run_s {
     cvg_u32 *hist_state = nullptr;
     cvg_u64 *lb = nullptr;        // look-back words of the one-pass allocation
     cvg_u32 *lb_ctl = nullptr;
+    cvg_u32 *tile_ctl = nullptr;  // the fill's warp-tile counter and CTA-done count
     cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
     cvg_acc_dev *acc = nullptr;
@@ -174,8 +176,18 @@ void write_file(const std::string &p, const std::vector<char> &data)
 }
 
 struct variant_key {
-    int dim, prec, block, esm, hsm, replay, n_params, grad, abi, nbins, minb;
+    int dim, prec, block, esm, hsm, replay, n_params, grad, abi, nbins, minb, wt;
 };
+
+// Tile shape of single-run fills: CVG_FILL_WARP_TILES=1 in the environment
+// forces warp tiles, =0 block tiles (the whole CTA on one tile of block*spt
+// samples, a barrier between tiles); unset (-1), a run chooses by its size.
+int env_warp_tiles()
+{
+    const char *e = std::getenv("CVG_FILL_WARP_TILES");
+    if (!e || !*e) return -1;
+    return e[0] == '0' ? 0 : 1;
+}
 
 // Integrand adaptor type F of the fill templates: static f (value) and df
 // (gradient w.r.t. theta) forwarding to the user's `integrand` /
@@ -206,6 +218,7 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     std::string s;
     s += "#define CVG_JIT 1\n";
     if (k.minb >= 2) s += "#define CVG_FILL_LOWREG 1\n";
+    s += "#define CVG_FILL_WARP_TILES " + std::to_string(k.wt) + "\n";
     s += cvg_src_common;
     s += "\nstatic constexpr int cvg_n_dim = " + std::to_string(k.dim) + ";\n";
     s += "#line 1 \"integrand.cu\"\n";
@@ -361,10 +374,11 @@ cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v
     cvg_context ctx = r->ctx;
     const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
     variant_key k{r->f->dim, r->p.precision, r->block, r->esm, r->hsm, replay ? 1 : 0,
-                  r->f->n_params, grad ? 1 : 0, r->f->abi, r->p.n_intervals, 1};
+                  r->f->n_params, grad ? 1 : 0, r->f->abi, r->p.n_intervals, 1, r->wt};
     if (grad) k.hsm = 0;
     const cvg_u64 smem = cvg_fill_smem_bytes(k.dim, r->p.n_intervals, tsz, k.esm, k.hsm, k.grad,
-                                             r->TS, k.n_params, k.block);
+                                             r->TS, k.n_params, k.block,
+                                             r->wt ? k.block / 32 : 1);
     k.minb = cvg_internal_fill_minb(ctx, k.block, smem);
     CKS(jit_kernel(ctx, *r->f, k, &v->kernel, &v->pilot));
     const void *fn = (const void *)v->kernel;
@@ -381,11 +395,12 @@ cvg_status prepare_variant(cvg_run_s *r, bool replay, bool grad, fill_variant *v
 void choose_layout(cvg_run_s *r)
 {
     const int tsz = r->p.precision == CVG_PREC_FP32 ? 4 : 8;
-    const int budget = r->ctx->smem_optin;
+    const int budget = r->ctx->smem_optin - 256;   // the kernel's static shared words
     const int D = r->f->dim, N = r->p.n_intervals, P = r->f->n_params;
     const int opts[4][2] = {{1, 1}, {0, 1}, {1, 0}, {0, 0}};
     for (auto &o : opts) {
-        if (cvg_fill_smem_bytes(D, N, tsz, o[0], o[1], 0, r->TS, P, r->block) <= (cvg_u64)budget) {
+        if (cvg_fill_smem_bytes(D, N, tsz, o[0], o[1], 0, r->TS, P, r->block,
+                                r->wt ? r->block / 32 : 1) <= (cvg_u64)budget) {
             r->esm = o[0];
             r->hsm = o[1];
             return;
@@ -462,6 +477,7 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.counts = r->counts;
     a.grad = r->grad;
     a.status = r->status;
+    a.tile_ctl = r->tile_ctl;
     a.scale_exp = r->p.precision == CVG_PREC_FP32 ? r->scale_exp : nullptr;
     a.scale_ss = r->p.precision == CVG_PREC_FP32 ? r->scale_ss : nullptr;
     a.bin_exp = r->p.precision == CVG_PREC_FP32 ? r->bin_exp : nullptr;
@@ -861,31 +877,40 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     const int64_t nh0 = std::max<int64_t>(2, (int64_t)(1.0 / (double)r->n_cubes * (double)r->n_eval_it));
 
     // tile shape
+    const int wt_env = env_warp_tiles();
+    r->wt = wt_env != 0 ? 1 : 0;
     r->block = p.block > 0 ? p.block : 512;
     r->spt = p.spt > 0 ? p.spt : 8;
     if (r->block % 32 || r->block > 1024) { delete r; return fail(CVG_ERR_INVALID, "block must be a multiple of 32, <= 1024"); }
     if (r->spt < 1 || r->spt > 256) { delete r; return fail(CVG_ERR_INVALID, "spt must be in [1, 256]"); }
+    const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8;
+    auto ctas = [&](int spt) {   // fill CTAs per SM that shared memory allows
+        const int TS = r->wt ? 32 * spt : r->block * spt;
+        for (auto &o : {std::pair<int, int>{1, 1}, {0, 1}, {1, 0}, {0, 0}}) {
+            const cvg_u64 b = cvg_fill_smem_bytes(D, p.n_intervals, tsz, o.first, o.second, 0, TS,
+                                                  f->n_params, r->block,
+                                                  r->wt ? r->block / 32 : 1);
+            if (b + 256 <= (cvg_u64)ctx->smem_optin) return (int)(ctx->smem_per_sm / (b + 1024));
+        }
+        return 0;
+    };
     if (p.spt <= 0) {
         // default: 16 samples per thread (half the per-tile staging of 8;
         // measured 4 % faster at d = 8 and d = 16) unless the larger
-        // cube-start table costs a CTA per SM
-        const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8, N = p.n_intervals;
-        auto ctas = [&](int spt) {
-            const int TS = r->block * spt;
-            for (auto &o : {std::pair<int, int>{1, 1}, {0, 1}, {1, 0}, {0, 0}}) {
-                const cvg_u64 b = cvg_fill_smem_bytes(D, N, tsz, o.first, o.second, 0, TS,
-                                                      f->n_params, r->block);
-                if (b <= (cvg_u64)ctx->smem_optin) return (int)(ctx->smem_per_sm / (b + 1024));
-            }
-            return 0;
-        };
-        // ... and unless the iteration has too few tiles to give every CTA of
+        // cube-start table costs a CTA per SM ... and unless the iteration has too few tiles to give every CTA of
         // the persistent grid several (small runs keep more, smaller tiles)
         const cvg_u64 tiles16 = s_max / ((cvg_u64)r->block * 16);
         const int c16 = ctas(16);
         if (c16 >= ctas(8) && c16 > 0 && tiles16 >= 4ull * (cvg_u64)c16 * ctx->n_sm) r->spt = 16;
     }
-    r->TS = r->block * r->spt;
+    // warp tiles pay off when every warp of the persistent grid gets several
+    // (measured on GB300: d=8, 1e8 samples, fill 1.870 -> 1.758 ms; d=4,
+    // 1e6 samples, one or two tiles per warp, 0.029 -> 0.031 ms)
+    if (r->wt && wt_env < 0) {
+        const cvg_u64 warps = (cvg_u64)std::max(1, ctas(r->spt)) * ctx->n_sm * (r->block / 32);
+        if (s_max / (32ull * r->spt) < 4ull * warps) r->wt = 0;
+    }
+    r->TS = r->wt ? 32 * r->spt : r->block * r->spt;
     r->max_tiles = (s_max + r->TS - 1) / r->TS + 1;
     r->nb = cvg_realloc_blocks(r->n_cubes);
     choose_layout(r);
@@ -919,6 +944,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->hist_state, 2 * sizeof(cvg_u32)},
         {(void **)&r->lb, sizeof(cvg_u64) * r->nb},
         {(void **)&r->lb_ctl, 2 * sizeof(cvg_u32)},
+        {(void **)&r->tile_ctl, 2 * sizeof(cvg_u32)},
         {(void **)&r->done, 2 * sizeof(cvg_u32)},
         {(void **)&r->theta, sizeof(double) * std::max(1, f->n_params)},
         {(void **)&r->grad, sizeof(double) * std::max(1, f->n_params)},
@@ -962,6 +988,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     CK(cudaMemsetAsync(r->done, 0, 2 * sizeof(cvg_u32), st));
     CK(cudaMemsetAsync(r->lb, 0, sizeof(cvg_u64) * r->nb, st));
     CK(cudaMemsetAsync(r->lb_ctl, 0, 2 * sizeof(cvg_u32), st));
+    CK(cudaMemsetAsync(r->tile_ctl, 0, 2 * sizeof(cvg_u32), st));
     // the first fill keeps float bin sums: the pilot's ~150 samples per bin
     // cannot bound the mean of a heavy-tailed bin (a d=16 Gaussian lost 2.8 %
     // of a dimension's sum to fixed point on the pilot's table); fixed point
@@ -1404,12 +1431,14 @@ cvg_status cvg_compile_check(const char *source, int32_t n_dim, int32_t abi, int
         // the default launch shape of a run (512 threads, 8 samples each,
         // 1024 bins, grid and histograms in shared memory when they fit)
         const int tsz = precision == CVG_PREC_FP32 ? 4 : 8;
-        variant_key k{n_dim, precision, 512, 1, g ? 0 : 1, 0, n_params, g, abi, 1024, 1};
-        if (cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, 4096, n_params, 512) > 232448)
+        variant_key k{n_dim, precision, 512, 1, g ? 0 : 1, 0, n_params, g, abi, 1024, 1,
+                      env_warp_tiles() != 0 ? 1 : 0};
+        const int TS = k.wt ? 32 * 16 : 512 * 16, groups = k.wt ? 16 : 1;
+        if (cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, TS, n_params, 512, groups) > 232448)
             k.hsm = 0;
         k.minb = cvg_internal_fill_minb(nullptr, 512,
-                                        cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, 4096,
-                                                            n_params, 512));
+                                        cvg_fill_smem_bytes(n_dim, 1024, tsz, 1, k.hsm, g, TS,
+                                                            n_params, 512, groups));
         std::vector<char> cubin;
         std::string l;
         st = nvrtc_cubin(make_source(f, k), nvrtc_options(arch), cubin, l);

@@ -106,6 +106,37 @@ def test_fill_fp32_histograms_every_dimension(ctx, dim, n_it, N, fixed):
     np.testing.assert_allclose(JF.sum(), o.JF.sum(), rtol=1e-5)
 
 
+@pytest.mark.parametrize("wt", ["1", "0"])
+@pytest.mark.parametrize("prec", [L.PREC_FP64, L.PREC_FP32])
+def test_warp_and_block_tiles(ctx, monkeypatch, wt, prec):
+    """The fill's two tile shapes (a warp's 32*spt samples claimed from a
+    counter, or the CTA's block*spt samples): the first fill's per-bin counts
+    against the oracle's, and for FP64 whole iterations against the oracle's."""
+    monkeypatch.setenv("CVG_FILL_WARP_TILES", wt)
+    # 2e6 samples: more warp tiles (256 samples) than the grid's warps, so
+    # warps also claim tiles from the counter
+    dim, n_it, N, it = 5, 2000000, 128, 4
+    kind = P.U_PHILOX_F64 if prec == L.PREC_FP64 else P.U_PHILOX_F32
+    with make_run(ctx, I.GAUSS, dim, n_it, it, N=N, seed=3, prec=prec, skip=1) as r:
+        r.step(L.STAGE_FILL)
+        Cn = r.get(L.BUF_COUNTS)
+        r.step(L.STAGE_REALLOC | L.STAGE_REFINE)
+        r.iterate(it - 1)
+        res, it_res, _ = r.result()
+    o = oracle_run(dim, n_it, it, N)
+    u, _ = P.uniforms(kind, seed=3)
+    S = o.fill(P.F_GAUSS, GAUSS_TH, u, it=0)
+    assert Cn.astype(np.int64).sum() == S * dim
+    if prec == L.PREC_FP64:
+        assert np.array_equal(Cn.astype(np.int64), o.counts)
+        u, _ = P.uniforms(P.U_PHILOX_F64, seed=3)
+        ref = P.integrate(P.F_GAUSS, dim, n_it * it, it, theta=GAUSS_TH, skip=1, n_intervals=N, u=u)
+        assert relerr(it_res, ref["it_res"]) < 1e-9
+    else:
+        assert np.abs(Cn.astype(np.int64) - o.counts).sum() <= 2e-4 * S * dim
+        assert abs(res.result - 1.0) < 5 * res.error
+
+
 def test_fp32_bin_exponent_table(ctx):
     """The pilot's table of per-bin weight exponents follows the integrand:
     central bins of the Gaussian far above the tails; each refinement
