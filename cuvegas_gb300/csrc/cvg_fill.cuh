@@ -245,6 +245,15 @@ CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
     const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
     return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
 }
+// 2^(16-e) for a bin exponent e in [-100, 100]: the float bits (143 - e) << 23
+// formed as one integer multiply-add (FMA pipe) instead of an add and a shift
+// (ALU, the fill's busiest pipe): measured 1.5 % off the d=8 fill.
+CVG_D float cvg_pow2_16me(int e)
+{
+    int b;
+    asm("mad.lo.s32 %0, %1, -8388608, 1199570944;" : "=r"(b) : "r"(e));
+    return __int_as_float(b);
+}
 // One fixed-point value update of bin i (exponent e, scaled weight s and
 // s + 2^23 in qf); the same steps as cvg_hist_add<true>.
 CVG_D cvg_u32 cvg_hist_put(float *hw, double *gw, int i, int e, float s, float qf, float w)
@@ -277,8 +286,7 @@ CVG_D cvg_u32 cvg_hist_group(float *hw, cvg_u32 *hc, double *gw, const int *i, f
 #pragma unroll
     for (int k = 0; k < G; k += 2) {
         const cvg_f32x2 s2 = cvg_mul2(cvg_pack2(w, w),
-                                      cvg_pack2(__int_as_float((143 - e[k]) << 23),
-                                                __int_as_float((143 - e[k + 1]) << 23)));
+                                      cvg_pack2(cvg_pow2_16me(e[k]), cvg_pow2_16me(e[k + 1])));
         cvg_unpack2(s2, s[k], s[k + 1]);
         cvg_unpack2(cvg_add2(s2, cvg_pack2(C, C)), q[k], q[k + 1]);
     }
@@ -907,18 +915,19 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
         constexpr int W = BS / 32;
         if (tid == 0) claimed = (cvg_u32)(W * TS);
         __syncthreads();
+        // (tile numbers fit 32 bits: an iteration holds < 2^31 samples)
         const cvg_u32 lane = tid & 31;
-        const cvg_u64 n_warps = (cvg_u64)gridDim.x * W;
-        auto claim = [&]() -> cvg_u64 {
+        const cvg_u32 n_warps = gridDim.x * W, nt = (cvg_u32)n_tiles;
+        auto claim = [&]() -> cvg_u32 {
             cvg_u32 t = 0xFFFFFFFFu;
             if (lane == 0 && atomicAdd(&claimed, (cvg_u32)TS) + (cvg_u32)TS <= CVG_HIST_MAX_RUN)
                 t = atomicAdd(&a.tile_ctl[0], 1u);
             t = __shfl_sync(0xffffffffu, t, 0);
-            return t == 0xFFFFFFFFu ? ~0ull : n_warps + t;
+            return t >= nt - n_warps ? 0xFFFFFFFFu : n_warps + t;
         };
-        cvg_u64 tile = (cvg_u64)blockIdx.x * W + (tid >> 5);
-        while (tile < n_tiles) {
-            const cvg_u64 next = n_warps < n_tiles ? claim() : ~0ull;
+        cvg_u32 tile = blockIdx.x * W + (tid >> 5);
+        while (tile < nt) {
+            const cvg_u32 next = n_warps < nt ? claim() : 0xFFFFFFFFu;
             if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX, true>(
                     a, sm, cx, tile, n_tiles, S, gacc, nrare, a.keys))
                 break;
