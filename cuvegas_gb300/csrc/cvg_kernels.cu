@@ -514,10 +514,7 @@ __device__ __forceinline__ cvg_u32 lb_next_epoch(cvg_u32 e) { return e % 0x3FFFF
 template <int MODE>
 __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
 {
-    __shared__ cvg_u32 sh[CVG_REALLOC_CHUNK];
-    __shared__ cvg_u64 st[CVG_REALLOC_CHUNK];
     __shared__ cvg_u64 scratch[33];
-    __shared__ cvg_u64 wtot[RB / 32];
     __shared__ unsigned s_blk;
     __shared__ cvg_u32 s_epoch;
     __shared__ cvg_u64 s_excl;
@@ -533,36 +530,51 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
     const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
     const cvg_u32 cnt = min((cvg_u32)CVG_REALLOC_CHUNK, a.n_cubes - base);
 
-    // n_h of this chunk (as k3_count)
+    // n_h of this thread's RIPT consecutive hypercubes, in registers (as k3_count)
     double dsum = 0.0, n_it = 0.0;
     float scale = 0.f;
     if (MODE == 0) { dsum = a.acc->dh_sum; n_it = (double)a.n_eval_it; }
     if (MODE == 2) scale = d2f_bits(a.acc->nh_scale) * 0.99999905f;
     const float *dh32 = reinterpret_cast<const float *>(a.dh);
+    const int i0 = tid * RIPT;
+    const cvg_u32 c0 = base + (cvg_u32)i0;
+    static_assert(RIPT == 8, "k3_alloc loads 8 hypercubes per thread");
+    cvg_u32 nh[RIPT];
+    const bool full = (cvg_u32)i0 + RIPT <= cnt;
+    if (MODE == 2 && full) {   // 32 contiguous bytes per thread
+        const float4 v0 = *reinterpret_cast<const float4 *>(dh32 + c0);
+        const float4 v1 = *reinterpret_cast<const float4 *>(dh32 + c0 + 4);
+        const float x[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-    for (int k = 0; k < RIPT; ++k) {
-        const int i = k * RB + tid;
-        const cvg_u32 c = base + i;
-        cvg_u32 nh = 0u;
-        if ((cvg_u32)i < cnt) {
-            if (MODE == 0) {
-                const double x = a.dh[c] / dsum * n_it;
-                int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
-                nh = ns < 2 ? 2u : (cvg_u32)ns;
-            } else if (MODE == 2) {
-                const float x = dh32[c] * scale;
-                const int ns = (x >= 0.f && x < 2147483520.f) ? (int)x : (x >= 2147483520.f ? 2147483520 : 0);
-                nh = ns < 2 ? 2u : (cvg_u32)ns;
-            } else {
-                nh = a.nh_new[c];
-            }
+        for (int k = 0; k < RIPT; ++k) {
+            const float y = x[k] * scale;
+            const int ns = (y >= 0.f && y < 2147483520.f) ? (int)y : (y >= 2147483520.f ? 2147483520 : 0);
+            nh[k] = ns < 2 ? 2u : (cvg_u32)ns;
         }
-        sh[i] = nh;
+    } else {
+#pragma unroll
+        for (int k = 0; k < RIPT; ++k) {
+            const cvg_u32 c = c0 + k;
+            cvg_u32 v = 0u;
+            if ((cvg_u32)(i0 + k) < cnt) {
+                if (MODE == 0) {
+                    const double x = a.dh[c] / dsum * n_it;
+                    int ns = (x >= 0.0 && x < 2147483647.0) ? (int)x : (x >= 2147483647.0 ? 2147483647 : 0);
+                    v = ns < 2 ? 2u : (cvg_u32)ns;
+                } else if (MODE == 2) {
+                    const float y = dh32[c] * scale;
+                    const int ns = (y >= 0.f && y < 2147483520.f) ? (int)y : (y >= 2147483520.f ? 2147483520 : 0);
+                    v = ns < 2 ? 2u : (cvg_u32)ns;
+                } else {
+                    v = a.nh_new[c];
+                }
+            }
+            nh[k] = v;
+        }
     }
-    __syncthreads();
     cvg_u64 local = 0;
 #pragma unroll
-    for (int k = 0; k < RIPT; ++k) local += sh[tid * RIPT + k];
+    for (int k = 0; k < RIPT; ++k) local += nh[k];
     cvg_u64 off = local;
     const cvg_u64 agg = block_exscan_u64(off, scratch);
 
@@ -604,17 +616,33 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
     __syncthreads();
     off += s_excl;
 
-    // prefixes and tile map (as k3_apply)
-    k3_prefix_tiles(a, sh, st, off, base, cnt);
-    __syncthreads();
-    for (int i = tid; i < (int)cnt; i += RB) a.nh_sum[base + i] = st[i];
+    // prefixes and tile map from registers (as k3_apply): one division per
+    // thread, the tile index then only advances
+    const cvg_u64 TS = (cvg_u64)a.tile_samples;
+    cvg_u64 t = (off + TS - 1) / TS;
+    cvg_u64 ts = t * TS;
+    cvg_u64 pre[RIPT];
+#pragma unroll
+    for (int k = 0; k < RIPT; ++k) {
+        pre[k] = off;
+        for (; ts < off + nh[k] && t < a.max_tiles; ++t, ts += TS) a.tile_cube[t] = c0 + k;
+        off += nh[k];
+    }
+    if (full) {   // 64 contiguous bytes per thread
+#pragma unroll
+        for (int k = 0; k < RIPT; k += 2)
+            *reinterpret_cast<ulonglong2 *>(a.nh_sum + c0 + k) = make_ulonglong2(pre[k], pre[k + 1]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < RIPT; ++k)
+            if ((cvg_u32)(i0 + k) < cnt) a.nh_sum[c0 + k] = pre[k];
+    }
     if (blk == nb - 1 && tid == 0) {
         // every block has taken its ticket: reset it; the next launch's epoch
         a.nh_sum[a.n_cubes] = s_excl + agg;
         a.lb_ctl[0] = 0u;
         a.lb_ctl[1] = epoch;
     }
-    (void)wtot;
 }
 
 
