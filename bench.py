@@ -527,11 +527,21 @@ def run_workload(args):
                          "frac_within_4sigma": float(np.mean(pulls < 4)),
                          "max_pull": float(pulls.max())}
         # plain form: FP64, one integral per call (the reference's interface shape)
-        for d in range(2, 13):    # compile every dimension first (JIT is not timed)
-            fi = ctx.integrand(I.PRODPEAK, d, n_params=2 * d)
-            runtime.integrate_once(fi, runtime.make_params(d, 4 * 4000, 4, skip=1,
-                                                           precision=L.PREC_FP64),
-                                   np.ones(2 * d))
+        # compile every dimension's fill first, in both tile shapes (a run
+        # picks warp tiles when its iterations are large), so no JIT is timed
+        saved = os.environ.get("CVG_FILL_WARP_TILES")
+        for wt in ("0", "1"):
+            os.environ["CVG_FILL_WARP_TILES"] = wt
+            for d in range(2, 13):
+                fi = ctx.integrand(I.PRODPEAK, d, n_params=2 * d)
+                runtime.integrate_once(fi, runtime.make_params(d, 4 * 4000, 4, skip=1,
+                                                               n_intervals=1024,
+                                                               precision=L.PREC_FP64),
+                                       np.ones(2 * d))
+        if saved is None:
+            del os.environ["CVG_FILL_WARP_TILES"]
+        else:
+            os.environ["CVG_FILL_WARP_TILES"] = saved
         t0 = time.perf_counter()
         ev_p = 0
         n_plain = 64
