@@ -68,7 +68,8 @@ class RunInfo(C.Structure):
                 ("max_tiles", C.c_int64), ("n_strat", C.c_int32), ("n_intervals", C.c_int32),
                 ("n_dim", C.c_int32), ("block", C.c_int32), ("spt", C.c_int32),
                 ("grid", C.c_int32), ("edges_smem", C.c_int32), ("hist_smem", C.c_int32),
-                ("v_cubes", C.c_double), ("fill_smem_bytes", C.c_int64)]
+                ("v_cubes", C.c_double), ("fill_smem_bytes", C.c_int64),
+                ("tile_samples", C.c_int32), ("warp_tiles", C.c_int32)]
 
 
 _lib = None

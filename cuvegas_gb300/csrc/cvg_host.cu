@@ -1270,6 +1270,8 @@ cvg_status cvg_run_info_get(cvg_run r, cvg_run_info *o)
     o->hist_smem = r->hsm;
     o->v_cubes = r->v_cubes;
     o->fill_smem_bytes = (int64_t)r->fill.smem;
+    o->tile_samples = r->TS;
+    o->warp_tiles = r->wt;
     return CVG_OK;
 }
 

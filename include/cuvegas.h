@@ -189,6 +189,8 @@ typedef struct {
     int32_t n_strat, n_intervals, n_dim, block, spt, grid, edges_smem, hist_smem;
     double v_cubes;
     int64_t fill_smem_bytes;
+    int32_t tile_samples;  /* samples per fill tile: 32*spt (warp tiles) or block*spt */
+    int32_t warp_tiles;    /* 1: each warp claims its own tiles; 0: the CTA shares one */
 } cvg_run_info;
 cvg_status cvg_run_info_get(cvg_run r, cvg_run_info *out);
 

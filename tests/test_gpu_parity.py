@@ -118,6 +118,8 @@ def test_warp_and_block_tiles(ctx, monkeypatch, wt, prec):
     dim, n_it, N, it = 5, 2000000, 128, 4
     kind = P.U_PHILOX_F64 if prec == L.PREC_FP64 else P.U_PHILOX_F32
     with make_run(ctx, I.GAUSS, dim, n_it, it, N=N, seed=3, prec=prec, skip=1) as r:
+        assert r.info.warp_tiles == int(wt)
+        assert r.info.tile_samples == (32 if wt == "1" else r.info.block) * r.info.spt
         r.step(L.STAGE_FILL)
         Cn = r.get(L.BUF_COUNTS)
         r.step(L.STAGE_REALLOC | L.STAGE_REFINE)
@@ -160,14 +162,15 @@ def test_fp32_bin_exponent_table(ctx):
 
 def test_fill_fp32_histogram_word_wraps(ctx):
     """f = 1 on the uniform grid: every sample adds weight 1 (2^16 fixed-point
-    units) to its bin.  A tile of 65536 consecutive samples (16384 cubes) lies
-    in one bin and puts 2^32 units in it, so its shared-memory word wraps; the
-    bin sums must still equal the counts exactly."""
+    units) to its bin.  Each CTA takes ~2.6e5 of the 4e7 samples, more than
+    2^16 per bin of its two, so its shared-memory words wrap (2^32 units)
+    at least once; the bin sums must still equal the counts exactly."""
     n_it = 40_000_000
     with make_run(ctx, I.CONST_ONE, 1, n_it, 2, N=2, seed=1, prec=L.PREC_FP32,
                   block=1024, spt=64) as r:
         assert int(r.get(L.BUF_SCALE_EXP)[0]) == 0
-        assert r.info.block * r.info.spt == 65536
+        assert r.info.grid <= 2 * 152
+        assert n_it / r.info.grid / 2 > 2 ** 16
         force_fixed_point(r)
         r.step(L.STAGE_FILL)
         W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
