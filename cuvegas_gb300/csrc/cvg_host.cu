@@ -910,6 +910,19 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         const cvg_u64 warps = (cvg_u64)std::max(1, ctas(r->spt)) * ctx->n_sm * (r->block / 32);
         if (s_max / (32ull * r->spt) < 4ull * warps) r->wt = 0;
     }
+    // warp tiles: larger tiles (fewer cube-start loads and searches per
+    // sample) where shared memory keeps the CTAs per SM, and one block of
+    // 1024 where two 512-thread CTAs would each be held to 64 registers
+    // anyway (one copy of the grid and histograms per SM leaves room for
+    // the larger cube-start buffers).  Measured on GB300, fill ms: d=8 1e8
+    // FP32 512x16 1.720, 1024x16 1.695, 1024x24 1.674, 1024x32 1.663; d=16
+    // 1e9 FP32 512x16 26.16, 512x24 25.72, 512x32 25.50.
+    if (r->wt && p.block <= 0 && p.spt <= 0) {
+        if (ctas(16) >= 2) r->block = 1024;
+        const int base = ctas(16);
+        for (int s : {32, 24})
+            if (base > 0 && ctas(s) >= base) { r->spt = s; break; }
+    }
     r->TS = r->wt ? 32 * r->spt : r->block * r->spt;
     r->max_tiles = (s_max + r->TS - 1) / r->TS + 1;
     r->nb = cvg_realloc_blocks(r->n_cubes);
