@@ -18,6 +18,9 @@ from . import _lib as L
 from . import runtime
 
 CANDIDATES = [(256, 16), (512, 8), (512, 12), (512, 16), (1024, 4), (1024, 8)]
+# single runs of large iterations run warp tiles (32 * spt samples per warp),
+# where larger tiles and 1024-thread blocks measured faster
+RUN_CANDIDATES = CANDIDATES + [(512, 24), (512, 32), (1024, 16), (1024, 24), (1024, 32)]
 _lock = threading.Lock()
 
 
@@ -62,7 +65,7 @@ def _key(kind, dims, prec, n_intervals, evals, source):
                                           prec, n_intervals, int(math.log2(max(evals, 1))))
 
 
-def tune_run(integrand, params, theta=None, candidates=CANDIDATES):
+def tune_run(integrand, params, theta=None, candidates=RUN_CANDIDATES):
     """Best (block, spt) for a single-instance run of these parameters."""
     key = _key("run", [params.n_dim], params.precision, params.n_intervals,
                params.tot_eval // params.max_it, integrand_source(integrand))

@@ -10,7 +10,9 @@
 // Work decomposition.  Samples of one iteration are numbered s = 0..S-1 in
 // cube order (cube c owns [nh_sum[c], nh_sum[c+1])), exactly the order of the
 // reference's evals[] array.  A persistent grid walks fixed-size tiles of
-// tile_samples consecutive samples; thread t of a tile owns spt consecutive
+// tile_samples consecutive samples, each taken by one warp (warp tiles,
+// claimed from a launch-wide counter) or by the whole CTA (block tiles, for
+// small iterations); thread t of a tile owns spt consecutive
 // samples, so a thread stays inside one cube for a run of samples and keeps
 // Sum f*jac and Sum (f*jac)^2 of that run in registers (compensated in FP32).
 // A run that starts and ends inside the thread's slice covers its whole cube
