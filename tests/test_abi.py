@@ -44,6 +44,18 @@ def test_integrands_compile(name, src, dim, P, g, prec):
     L.compile_check(src, dim, precision=prec, n_params=P, has_grad=g)
 
 
+@pytest.mark.parametrize("wt", ["0", "1"])
+@pytest.mark.parametrize("dim,P", [(3, 0), (8, 0), (16, 16)])
+def test_fill_tile_shapes_compile(monkeypatch, wt, dim, P):
+    """Both tile shapes of the single-run fill (warp tiles, block tiles)
+    compile for FP32 and FP64, with and without the gradient pass."""
+    monkeypatch.setenv("CVG_FILL_WARP_TILES", wt)
+    src = I.GAUSS if P == 0 else I.CORNER
+    for prec in (L.PREC_FP32, L.PREC_FP64):
+        L.compile_check(src, dim, precision=prec, n_params=P)
+    L.compile_check(I.MIXTURE, 6, precision=L.PREC_FP32, n_params=16, has_grad=True)
+
+
 def test_numba_abi_compiles():
     src = """extern "C" __device__ int integrand(double* ret, double* x) {
         double s = 0; for (int i = 0; i < cvg_n_dim; ++i) s += x[i]; *ret = s; return 0; }"""
