@@ -143,7 +143,6 @@ std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
 {
     const char *T = b.p.precision == CVG_PREC_FP32 ? "float" : "double";
     std::string s = "#define CVG_JIT 1\n";
-    if (cvg_internal_fill_minb(b.ctx, b.block, b.fill_smem) >= 2) s += "#define CVG_FILL_LOWREG 1\n";
     // the one-dimension-at-a-time map: measured faster in the batched
     // kernel, which holds every dimension's variant at once (22.7 against
     // 25.1 G evals/s with the packed pairs)

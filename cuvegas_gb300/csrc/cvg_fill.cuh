@@ -179,24 +179,20 @@ CVG_D int cvg_bin(double z, int N, double, double &frac)
 // 2^(e+7) (or non-finite) goes to the global FP64 sum directly.
 // FP64 form: FP64 atomics, sums in the reference's precision.
 // The FP32 map runs dimension pairs as packed f32x2 instructions
-// (CVG_FILL_PAIRS), and the fixed-point histogram updates go in groups with
-// their scale arithmetic in f32x2 pairs (CVG_HIST_PAIRS).
+// (CVG_FILL_PAIRS; the batched fill, which holds every dimension's variant in
+// one kernel, keeps one dimension at a time).
 #ifndef CVG_FILL_PAIRS
 #define CVG_FILL_PAIRS 1
 #endif
-#ifndef CVG_HIST_PAIRS
-#define CVG_HIST_PAIRS 1
-#endif
-// Histogram updates issued together (even; 0: 8) and their rare-path form
-// (1: a branch per update, 0: per group, 2 or -1: per sample).  Measured on
-// GB300 (fill ms, d=8 Gaussian 1e8 / d=16 corner 1e9): per update in pairs
-// 1.898 / -, per group of 4 - / 30.95, per sample in groups of 4
-// 1.875 / 30.52, of 8 1.869 / 29.57, of 16 - / 29.92.
+// The fixed-point histogram updates of a sample go in groups of
+// CVG_HIST_GROUP dimensions (then 4, 2, 1): count atomics together, scale
+// arithmetic in f32x2 pairs, rare updates of all dimensions behind one branch
+// per sample.  Measured on GB300 (fill ms, d=8 Gaussian 1e8 / d=16 corner
+// 1e9): scalar updates, a branch each 2.02 / 38.2; pairs, a branch per update
+// 1.94 / 33.9; groups of 4, a branch per group - / 30.95; one branch per
+// sample in groups of 4 1.875 / 30.52, of 8 1.869 / 29.57, of 16 - / 29.92.
 #ifndef CVG_HIST_GROUP
-#define CVG_HIST_GROUP 0
-#endif
-#ifndef CVG_HIST_BRANCHY
-#define CVG_HIST_BRANCHY -1
+#define CVG_HIST_GROUP 8
 #endif
 #define CVG_HIST_CNT_MASK 0x00FFFFFFu
 #define CVG_HIST_MAX_RUN 0x00FFF000u   // samples between flushes (counts < 2^24)
@@ -210,42 +206,16 @@ template <int D, typename T> CVG_D constexpr bool cvg_hist_fixed()
     return sizeof(T) == 4 && D <= CVG_HIST_FIX_MAX_DIM;
 }
 
-// Returns 1 when the update took a rare path (a wrap or a large weight).
-template <bool FIX>
-CVG_D cvg_u32 cvg_hist_add(float *hw, cvg_u32 *hc, double *gw, int i, float w)
+// Float-form update of bin i (shared-memory float atomic and count).
+CVG_D void cvg_hist_add_float(float *hw, cvg_u32 *hc, int i, float w)
 {
-    if (!FIX) {
-        atomicAdd(hw + i, w);
-        atomicAdd(hc + i, 1u);
-        return 0u;
-    }
-    const cvg_u32 old = atomicAdd(hc + i, 1u);
-    const int e = (int)old >> 24;                             // this bin's scale exponent
-    const float s = w * __int_as_float((143 - e) << 23);      // w * 2^(16-e)
-    if (s < 8388608.0f) {   // round-to-nearest integer by a 2^23 add (no conversion instruction)
-        const cvg_u32 q = __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u;
-        const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
-        if (o + q < o) {
-            atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
-            return 1u;
-        }
-        return 0u;
-    }
-    atomicAdd(gw + i, cvg_f2d(w));
-    return 1u;
+    atomicAdd(hw + i, w);
+    atomicAdd(hc + i, 1u);
 }
-// Fixed-point update of bin i without branches: returns 1 if w did not fit
-// (the caller adds it to the global FP64 sum), 2 if the word wrapped (the
-// caller adds 2^(16+e)), 0 otherwise (almost always).
-CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
+CVG_D void cvg_hist_add_float(double *hw, cvg_u32 *hc, int i, double w)
 {
-    const cvg_u32 old = atomicAdd(hc + i, 1u);
-    const int e = (int)old >> 24;
-    const float s = w * __int_as_float((143 - e) << 23);      // w * 2^(16-e)
-    const bool fits = s < 8388608.0f;
-    const cvg_u32 q = fits ? __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u : 0u;
-    const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
-    return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
+    atomicAdd(hw + i, w);
+    atomicAdd(hc + i, 1u);
 }
 // 2^(16-e) for a bin exponent e in [-100, 100]: the float bits (143 - e) << 23
 // formed as one integer multiply-add (FMA pipe) instead of an add and a shift
@@ -256,29 +226,24 @@ CVG_D float cvg_pow2_16me(int e)
     asm("mad.lo.s32 %0, %1, -8388608, 1199570944;" : "=r"(b) : "r"(e));
     return __int_as_float(b);
 }
-// One fixed-point value update of bin i (exponent e, scaled weight s and
-// s + 2^23 in qf); the same steps as cvg_hist_add<true>.
-CVG_D cvg_u32 cvg_hist_put(float *hw, double *gw, int i, int e, float s, float qf, float w)
+// Fixed-point update of bin i without branches: returns 1 if w did not fit
+// (the caller adds it to the global FP64 sum), 2 if the word wrapped (the
+// caller adds 2^(16+e)), 0 otherwise (almost always).
+CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
 {
-    if (s < 8388608.0f) {
-        const cvg_u32 q = __float_as_uint(qf) - 0x4B000000u;
-        const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
-        if (o + q < o) {
-            atomicAdd(gw + i, __hiloint2double((1039 + e) << 20, 0));   // 2^(16+e)
-            return 1u;
-        }
-        return 0u;
-    }
-    atomicAdd(gw + i, cvg_f2d(w));
-    return 1u;
+    const int e = (int)atomicAdd(hc + i, 1u) >> 24;          // this bin's scale exponent
+    const float s = w * cvg_pow2_16me(e);                     // w * 2^(16-e)
+    const bool fits = s < 8388608.0f;
+    const cvg_u32 q = fits ? __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u : 0u;
+    const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
+    return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
 }
 // G updates (G even; bins i[0..G), one weight w): all count atomics first,
 // then the scale arithmetic in pairs, then the value atomics, so that G
-// shared-memory round trips overlap.  Returns the rare updates (branchy) or
-// leaves their codes in rare[] (branchless).
-template <int G, bool BRANCHY>
-CVG_D cvg_u32 cvg_hist_group(float *hw, cvg_u32 *hc, double *gw, const int *i, float w,
-                             cvg_u32 *rare)
+// shared-memory round trips overlap.  Leaves each update's rare code in
+// rare[] (as cvg_hist_add_fix).
+template <int G>
+CVG_D void cvg_hist_group(float *hw, cvg_u32 *hc, const int *i, float w, cvg_u32 *rare)
 {
     const float C = 8388608.0f;
     int e[G];
@@ -292,20 +257,13 @@ CVG_D cvg_u32 cvg_hist_group(float *hw, cvg_u32 *hc, double *gw, const int *i, f
         cvg_unpack2(s2, s[k], s[k + 1]);
         cvg_unpack2(cvg_add2(s2, cvg_pack2(C, C)), q[k], q[k + 1]);
     }
-    cvg_u32 n = 0;
-    if (BRANCHY) {
 #pragma unroll
-        for (int k = 0; k < G; ++k) n += cvg_hist_put(hw, gw, i[k], e[k], s[k], q[k], w);
-    } else {
-#pragma unroll
-        for (int k = 0; k < G; ++k) {
-            const bool f = s[k] < C;
-            const cvg_u32 u = f ? __float_as_uint(q[k]) - 0x4B000000u : 0u;
-            const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i[k], u);
-            rare[k] = (f ? 0u : 1u) | (o + u < o ? 2u : 0u);
-        }
+    for (int k = 0; k < G; ++k) {
+        const bool f = s[k] < C;
+        const cvg_u32 u = f ? __float_as_uint(q[k]) - 0x4B000000u : 0u;
+        const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i[k], u);
+        rare[k] = (f ? 0u : 1u) | (o + u < o ? 2u : 0u);
     }
-    return n;
 }
 CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, float w)
 {
@@ -313,9 +271,8 @@ CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, flo
     if (rare & 2u) atomicAdd(gw + i, __hiloint2double((1039 + ((int)hc[i] >> 24)) << 20, 0));
 }
 // Dimensions d0..d0+G-1 of one sample (bins bin[], weight w) through
-// cvg_hist_group; returns the number of rare updates.
-// The same with the rare codes of the group returned as 2-bit fields at
-// bit 2*(d0+k) of a per-sample mask (handled once per sample).
+// cvg_hist_group; the rare codes returned as 2-bit fields at bit 2*(d0+k) of
+// a per-sample mask.
 template <int G>
 CVG_D cvg_u32 cvg_fill_hist_group_mask(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
                                        const int *bin, float w)
@@ -324,39 +281,11 @@ CVG_D cvg_u32 cvg_fill_hist_group_mask(float *hw, cvg_u32 *hc, double *gw, int d
     cvg_u32 rare[G];
 #pragma unroll
     for (int k = 0; k < G; ++k) i[k] = (d0 + k) * N + bin[d0 + k];
-    cvg_hist_group<G, false>(hw, hc, gw, i, w, rare);
+    cvg_hist_group<G>(hw, hc, i, w, rare);
     cvg_u32 m = 0;
 #pragma unroll
     for (int k = 0; k < G; ++k) m |= rare[k] << (2 * (d0 + k));
     return m;
-}
-template <int G, bool BRANCHY>
-CVG_D cvg_u32 cvg_fill_hist_group(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
-                                  const int *bin, float w)
-{
-    int i[G];
-    cvg_u32 rare[G];
-#pragma unroll
-    for (int k = 0; k < G; ++k) i[k] = (d0 + k) * N + bin[d0 + k];
-    cvg_u32 n = cvg_hist_group<G, BRANCHY>(hw, hc, gw, i, w, rare);
-    if (!BRANCHY) {
-        cvg_u32 any = 0;
-#pragma unroll
-        for (int k = 0; k < G; ++k) any |= rare[k];
-        if (any) {
-#pragma unroll
-            for (int k = 0; k < G; ++k)
-                if (rare[k]) { cvg_hist_rare(hc, gw, i[k], rare[k], w); ++n; }
-        }
-    }
-    return n;
-}
-template <bool FIX>
-CVG_D cvg_u32 cvg_hist_add(double *hw, cvg_u32 *hc, double *, int i, double w)
-{
-    atomicAdd(hw + i, w);
-    atomicAdd(hc + i, 1u);
-    return 0u;
 }
 // Bin sum and count of a shared-memory histogram entry, in the units of the
 // global histogram.
@@ -746,70 +675,40 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                 const T jf = (T)F::f(x, sm.th) * jac;
                 const T jf2 = jf * jf;
                 if constexpr (H && FIX) {
-#if CVG_HIST_PAIRS
                     // fixed-point bin sums in groups of dimensions (count
                     // atomics together, scale arithmetic in f32x2 pairs); the
                     // rare updates (a wrap or a large weight) of all
                     // dimensions are collected in a mask and handled behind
-                    // one branch per sample
-                    constexpr int HG = CVG_HIST_GROUP > 0 ? CVG_HIST_GROUP : 8;
-                    constexpr int BR = CVG_HIST_BRANCHY >= 0 ? CVG_HIST_BRANCHY : 2;
-                    // groups of HG, then of 4 and 2, then one dimension
+                    // one branch per sample.  Groups of CVG_HIST_GROUP, then
+                    // of 4 and 2, then one dimension.
+                    static_assert(D <= 16, "2-bit rare codes of every dimension in 32 bits");
+                    constexpr int HG = CVG_HIST_GROUP;
                     constexpr int R0 = (D / HG) * HG;
                     constexpr int R1 = R0 + ((D - R0) / 4) * 4;
                     constexpr int R2 = R1 + ((D - R1) / 2) * 2;
-                    if constexpr (BR == 2 && D <= 16) {
-                        cvg_u32 m = 0;
+                    cvg_u32 m = 0;
 #pragma unroll
-                        for (int d0 = 0; d0 < R0; d0 += HG)
-                            m |= cvg_fill_hist_group_mask<HG>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                    for (int d0 = 0; d0 < R0; d0 += HG)
+                        m |= cvg_fill_hist_group_mask<HG>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
 #pragma unroll
-                        for (int d0 = R0; d0 < R1; d0 += 4)
-                            m |= cvg_fill_hist_group_mask<4>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
-                        if constexpr (R2 > R1)
-                            m |= cvg_fill_hist_group_mask<2>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
-                        if constexpr (D > R2)
-                            m |= cvg_hist_add_fix(sm.hw, sm.hc, R2 * N + bin[R2], jf2) << (2 * R2);
-                        if (m) {
+                    for (int d0 = R0; d0 < R1; d0 += 4)
+                        m |= cvg_fill_hist_group_mask<4>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                    if constexpr (R2 > R1)
+                        m |= cvg_fill_hist_group_mask<2>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
+                    if constexpr (D > R2)
+                        m |= cvg_hist_add_fix(sm.hw, sm.hc, R2 * N + bin[R2], jf2) << (2 * R2);
+                    if (m) {
 #pragma unroll
-                            for (int d = 0; d < D; ++d) {
-                                const cvg_u32 r = (m >> (2 * d)) & 3u;
-                                if (r) { cvg_hist_rare(sm.hc, a.weights, d * N + bin[d], r, jf2); ++nrare; }
-                            }
+                        for (int d = 0; d < D; ++d) {
+                            const cvg_u32 r = (m >> (2 * d)) & 3u;
+                            if (r) { cvg_hist_rare(sm.hc, a.weights, d * N + bin[d], r, jf2); ++nrare; }
                         }
-                    } else {
-#pragma unroll
-                        for (int d0 = 0; d0 < R0; d0 += HG)
-                            nrare += cvg_fill_hist_group<HG, BR == 1>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
-#pragma unroll
-                        for (int d0 = R0; d0 < R1; d0 += 4)
-                            nrare += cvg_fill_hist_group<4, BR == 1>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
-                        if constexpr (R2 > R1)
-                            nrare += cvg_fill_hist_group<2, BR == 1>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
-                        if constexpr (D > R2)
-                            nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights, R2 * N + bin[R2], jf2);
                     }
-#elif defined(CVG_FILL_LOWREG)
-                    // held to 64 registers (2 CTAs per SM): branches keep the
-                    // dimensions' updates apart and fewer values live
-#pragma unroll
-                    for (int d = 0; d < D; ++d)
-                        nrare += cvg_hist_add<true>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
-#else
-                    // fixed-point bin sums; a wrap or a large weight (rare) is
-                    // handled behind a single branch per dimension
-#pragma unroll
-                    for (int d = 0; d < D; ++d) {
-                        const int i = d * N + bin[d];
-                        const cvg_u32 rare = cvg_hist_add_fix(sm.hw, sm.hc, i, jf2);
-                        if (rare) { cvg_hist_rare(sm.hc, a.weights, i, rare, jf2); ++nrare; }
-                    }
-#endif
                 } else {
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
                         if (H) {
-                            cvg_hist_add<false>(sm.hw, sm.hc, a.weights, d * N + bin[d], jf2);
+                            cvg_hist_add_float(sm.hw, sm.hc, d * N + bin[d], jf2);
                         } else {
                             atomicAdd(&a.weights[d * N + bin[d]], cvg_to_double(jf2));
                             atomicAdd(&a.counts[d * N + bin[d]], 1u);

@@ -217,7 +217,6 @@ std::string make_source(const cvg_integrand_s &f, const variant_key &k)
     const char *T = k.prec == CVG_PREC_FP32 ? "float" : "double";
     std::string s;
     s += "#define CVG_JIT 1\n";
-    if (k.minb >= 2) s += "#define CVG_FILL_LOWREG 1\n";
     s += "#define CVG_FILL_WARP_TILES " + std::to_string(k.wt) + "\n";
     s += cvg_src_common;
     s += "\nstatic constexpr int cvg_n_dim = " + std::to_string(k.dim) + ";\n";
