@@ -13,9 +13,10 @@ Printed JSON line (rank 0):
   e2e        evals/s of whole integrations through the C ABI with host
              parameters in and host results out (cvg_integrate)
   plain      the same workload in the plain FP64 form
-  roofline   fill kernel: algorithmic FP32 ops per evaluation x evaluations
-             per launch / CUDA-event launch time, against a live FP32 FMA
-             microbenchmark of the same GPU
+  roofline   fill kernel against the lowest of its per-pipe ceilings (FP32
+             ops, ex2, Philox4x32-10 calls per evaluation), each peak from a
+             live microbenchmark of the same GPU; the sampler binds, so
+             achieved = Philox calls per launch / CUDA-event launch time
   cpu_baseline  the CPU oracle (FP64, OpenMP, all host cores) on a bounded
              sample of the same workload
 `--impl reference` times the reference's computation on the host cores (the
