@@ -113,11 +113,14 @@ def test_warp_and_block_tiles(ctx, monkeypatch, wt, prec):
     counter, or the CTA's block*spt samples): the first fill's per-bin counts
     against the oracle's, and for FP64 whole iterations against the oracle's."""
     monkeypatch.setenv("CVG_FILL_WARP_TILES", wt)
-    # 2e6 samples: more warp tiles (256 samples) than the grid's warps, so
-    # warps also claim tiles from the counter
+    # 2e6 samples in warp tiles of 32 x 8: more tiles than the grid's warps,
+    # so warps also claim tiles from the counter
     dim, n_it, N, it = 5, 2000000, 128, 4
     kind = P.U_PHILOX_F64 if prec == L.PREC_FP64 else P.U_PHILOX_F32
-    with make_run(ctx, I.GAUSS, dim, n_it, it, N=N, seed=3, prec=prec, skip=1) as r:
+    with make_run(ctx, I.GAUSS, dim, n_it, it, N=N, seed=3, prec=prec, skip=1,
+                  block=512, spt=8) as r:
+        if wt == "1":
+            assert n_it // r.info.tile_samples > r.info.grid * r.info.block // 32
         assert r.info.warp_tiles == int(wt)
         assert r.info.tile_samples == (32 if wt == "1" else r.info.block) * r.info.spt
         r.step(L.STAGE_FILL)
