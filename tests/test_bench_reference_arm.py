@@ -24,3 +24,25 @@ def test_reference_arm_json_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
     assert d["config"]["workload"] and d["metric"]
+
+
+def test_fill_roofline_binds_the_slowest_pipe():
+    """bench.fill_roofline: each pipe's ceiling in evaluations/s, the lowest
+    one binds, achieved and frac in that pipe's units."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class FakeCtx:
+        peaks = {0: 70.0, 8: 10.0, 9: 0.4}      # T FMA-flops/s, T ex2/s, T Philox calls/s
+
+        def measure_peak(self, kind):
+            return self.peaks[kind]
+
+    # 1e8 evaluations in 2 ms = 5e10 evals/s; 92 FP32 ops, 8 ex2, 2 Philox calls each
+    r = bench.fill_roofline(FakeCtx(), 1e8, 2.0, 92, 8, 2)
+    c = r["ceilings_evals_per_s"]
+    assert abs(c["fp32"] - 35e12 / 92) < 1 and abs(c["sfu"] - 10e12 / 8) < 1
+    assert abs(c["sampler"] - 0.4e12 / 2) < 1
+    assert r["bound"] == "sampler" and r["unit"] == "T Philox calls/s"
+    assert abs(r["achieved"] - 5e10 * 2 / 1e12) < 1e-12
+    assert abs(r["frac"] - 5e10 / 2e11) < 1e-12
