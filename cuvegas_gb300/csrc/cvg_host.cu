@@ -906,7 +906,10 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
     // (measured on GB300: d=8, 1e8 samples, fill 1.870 -> 1.758 ms; d=4,
     // 1e6 samples, one or two tiles per warp, 0.029 -> 0.031 ms)
     if (r->wt && wt_env < 0) {
-        const cvg_u64 warps = (cvg_u64)std::max(1, ctas(r->spt)) * ctx->n_sm * (r->block / 32);
+        // resident CTAs: shared memory, and registers at 64 per thread (the
+        // fill's launch bounds), whichever is fewer
+        const int res = std::max(1, std::min(ctas(r->spt), 65536 / (r->block * 64)));
+        const cvg_u64 warps = (cvg_u64)res * ctx->n_sm * (r->block / 32);
         if (s_max / (32ull * r->spt) < 4ull * warps) r->wt = 0;
     }
     // warp tiles: larger tiles (fewer cube-start loads and searches per
