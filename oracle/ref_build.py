@@ -13,8 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF = os.environ.get("CVG_REFERENCE", "/root/reference")
 DIMS = (2, 3, 4)
-# the reference's kernels for the benchmark workloads' Gaussian (width 0.1),
-# timed on the GPU by tests/golden/time_reference.py
+# the reference's kernels for the benchmark workloads' Gaussian (width 0.1):
+# golden vectors at the d=4 and d=8 benchmark shapes, and the reference-kernel
+# timing leg of bench.py
 TIMING = ((4, "0.1"), (8, "0.1"))
 
 

@@ -11,9 +11,10 @@
 // sequence as vegasFill (src/main.cu:28-46) on a copy of the generator states
 // taken just before the fill -- curand is called, not re-implemented.
 //
-// Usage: ref_harness <ptx> <dim> <n_eval_it> <n_intervals> <iters> <out_dir> [time]
+// Usage: ref_harness <ptx> <dim> <n_eval_it> <n_intervals> <iters> <out_dir> [time|keep=i,j,..]
 // With "time" nothing is dumped: each iteration (the reference's whole
 // sequence, its host reads included) is timed with CUDA events and printed.
+// With "keep=..." only the listed iterations are dumped (all are run).
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
@@ -21,6 +22,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <string>
@@ -83,7 +85,8 @@ static void launch(cudaKernel_t k, long n, int block, void **args)
 int main(int argc, char **argv)
 {
     if (argc != 7 && argc != 8) {
-        std::fprintf(stderr, "usage: %s ptx dim n_eval_it n_intervals iters out_dir [time]\n",
+        std::fprintf(stderr,
+                     "usage: %s ptx dim n_eval_it n_intervals iters out_dir [time|keep=i,j,..]\n",
                      argv[0]);
         return 1;
     }
@@ -94,7 +97,16 @@ int main(int argc, char **argv)
     const int iters = std::atoi(argv[5]);
     g_out = argv[6];
     const bool timing = argc > 7 && std::strcmp(argv[7], "time") == 0;
-    double alpha = 0.5, beta = 0.75;
+    std::vector<char> keep(iters > 0 ? iters : 1, 1);
+    if (argc > 7 && std::strncmp(argv[7], "keep=", 5) == 0) {
+        std::fill(keep.begin(), keep.end(), 0);
+        for (const char *c = argv[7] + 5; *c;) {
+            const int k = std::atoi(c);
+            if (k >= 0 && k < iters) keep[k] = 1;
+            while (*c && *c != ',') c++;
+            if (*c == ',') c++;
+        }
+    }    double alpha = 0.5, beta = 0.75;
     const long max_batch_size = 1048576;
 
     FILE *fp = std::fopen(ptx_path, "rb");
@@ -228,20 +240,21 @@ int main(int argc, char **argv)
         CK(cudaMemcpy(&last_nh, nh + n_cubes - 1, sizeof(long), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(&last_sum, nh_sum + n_cubes - 1, sizeof(long), cudaMemcpyDeviceToHost));
         long idx = last_sum + last_nh;
-        if (!timing) {
+        const bool dumping = !timing && keep[it];
+        if (dumping) {
             dump("nh", it, nh, n_cubes);
             dump("x_edges_in", it, x_edges, (size_t)n_dim * n_edges);
         }
         // fill (src/main.cu:618-628)
         int runs = idx / batch_size + (int)((idx % batch_size) != 0);
-        if (!timing)
+        if (dumping)
             CK(cudaMemcpy(states_copy, states, sizeof(curandState) * batch_size, cudaMemcpyDeviceToDevice));
         {
             void *a[] = {&n_strat, &n_intervals, &n_edges, &idx, &batch_size, &runs, &counts,
                          &weights, &x_edges, &dx_edges, &JF, &JF2, &evals, &states};
             launch(k_fill, batch_size, 64, a);
         }
-        if (!timing) {
+        if (dumping) {
             dump_uniforms<<<(unsigned)((batch_size + 127) / 128), 128>>>(states_copy, n_dim, idx,
                                                                        batch_size, runs, ubuf);
             CK(cudaGetLastError());
@@ -302,7 +315,7 @@ int main(int argc, char **argv)
             double r = 0.0;
             CK(cudaMemcpy(&r, res_s, sizeof(double), cudaMemcpyDeviceToHost));
             std::printf("iteration %d samples %ld ms %.4f estimate %.9f\n", it, idx, ms, r);
-        } else {
+        } else if (dumping) {
             dump("dh", it, dh, n_cubes);
             dump("nh_next", it, nh, n_cubes);
             dump("x_edges_out", it, x_edges, (size_t)n_dim * n_edges);

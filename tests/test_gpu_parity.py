@@ -291,6 +291,92 @@ def test_full_run_fp64_matches_oracle(ctx, graph):
     np.testing.assert_allclose(xe, o["x_edges"], rtol=1e-9, atol=1e-12)
 
 
+@pytest.mark.parametrize("dim,n_it,max_it,skip", [(4, 1_000_000, 10, 5), (8, 2_000_000, 4, 1)],
+                         ids=["c1_d4_1e6x10", "c2shape_d8_2e6x4"])
+def test_benchmark_shape_full_run_fp64_matches_oracle(ctx, dim, n_it, max_it, skip):
+    """C1 exactly (d=4, 1e6 evals/iteration, 10 iterations, 1024 bins, alpha
+    0.5, beta 0.75, seed 0) and the d=8 / 1024-bin shape of the headline at
+    2e6 evals/iteration, FP64 form, through the C ABI against the oracle on
+    the same Philox stream: identical evaluation totals, every iteration's
+    estimate to 1e-9, the result to 1e-10 and the final grid to 1e-9."""
+    N = 1024
+    with make_run(ctx, I.GAUSS, dim, n_it, max_it, N=N, seed=0, skip=skip) as r:
+        r.iterate(max_it)
+        res, it_res, it_sig = r.result()
+        xe = r.get(L.BUF_X_EDGES)
+    u, _ = P.uniforms(P.U_PHILOX_F64, seed=0)
+    o = P.integrate(P.F_GAUSS, dim, n_it * max_it, max_it, theta=GAUSS_TH, skip=skip,
+                    n_intervals=N, u=u)
+    assert res.tot_nevals == o["tot_nevals"]
+    assert relerr(it_res, o["it_res"]) < 1e-9
+    assert relerr(it_sig, o["it_sig"]) < 1e-8
+    assert abs(res.result - o["result"]) / abs(o["result"]) < 1e-10
+    assert abs(res.error - o["error"]) / o["error"] < 1e-8
+    np.testing.assert_allclose(xe, o["x_edges"], rtol=1e-9, atol=1e-12)
+
+
+def _quantiles(a):
+    a = np.asarray(a, dtype=np.float64)
+    return {"p50": float(np.median(a)), "p99": float(np.quantile(a, 0.99)),
+            "p999": float(np.quantile(a, 0.999)), "max": float(a.max()), "n": int(a.size)}
+
+
+@pytest.mark.parametrize("dim,n_it,pre", [(4, 1_000_000, 3), (4, 1_000_000, 9), (8, 2_000_000, 3)],
+                         ids=["c1_it3", "c1_it9", "c2shape_it3"])
+def test_fp32_elementwise_against_fp64_oracle(ctx, record_property, dim, n_it, pre):
+    """Chosen (FP32-compensated) form against the FP64 oracle, element by
+    element, on the same Philox samples: the FP32 loop adapts for `pre`
+    iterations, then its next fill (fixed-point bin sums) is compared with the
+    oracle's fill of the same iteration on the same grid and n_h.
+
+    Measured on GB300 at these shapes: per-hypercube JF and JF2 agree to a
+    median of ~5e-5 / 1e-4 and a 99.9th percentile of ~6e-4 / 1.2e-3 relative;
+    per-bin weights to a median of ~7e-5 and a 99th percentile of ~1e-3.
+    The FP32 map takes bin widths from FP32 edges (for the narrowest adapted
+    bins the width differs from the FP64 width by ~3e-4 relative; the map and
+    its Jacobian stay consistent, so the estimate stays unbiased), and a
+    sample whose y*N lies within FP32 rounding of a bin edge lands in the
+    neighbouring bin (the largest per-cube differences, up to ~0.2 in a cube
+    of few samples).  Hypercubes whose per-sample (f*jac*2^-k)^2 fall below
+    the FP32 range (JF2/n < 2^-80 after scaling) flush to zero in the FP32
+    sums; together they hold less than 1e-12 of the integral and are
+    excluded from the per-cube figures.  Bounds asserted: JF median 3e-4,
+    99.9th percentile 3e-3, max 0.5; JF2 median 6e-4, 99.9th percentile 6e-3,
+    max 0.5; weights median 3e-4, 99th percentile 5e-3, max 0.05 over bins
+    above 1e-20 of the largest; bin counts within 2e-4 of all updates; sum
+    of JF within 2e-6."""
+    N = 1024
+    with make_run(ctx, I.GAUSS, dim, n_it, 10, N=N, seed=0, prec=L.PREC_FP32, skip=0) as r:
+        r.iterate(pre)
+        xe, nh = r.get(L.BUF_X_EDGES), r.get(L.BUF_NH)
+        assert r.get(L.BUF_HIST_STATE)[0] == 1          # fixed-point bin sums
+        r.step(L.STAGE_FILL)
+        JF, JF2 = r.get(L.BUF_JF), r.get(L.BUF_JF2)
+        W, Cn = r.get(L.BUF_WEIGHTS), r.get(L.BUF_COUNTS)
+        k = int(r.get(L.BUF_BIN_EXP)[-1])
+    W = W * 4.0 ** k
+    o = P.OracleRun(dim, n_it * 10, 10, n_intervals=N)
+    o.set_x_edges(xe)
+    o.set_nh(nh.astype(np.int64))
+    u, _ = P.uniforms(P.U_PHILOX_F32, seed=0)
+    S = o.fill(P.F_GAUSS, GAUSS_TH, u, it=pre)
+    oJF, oJF2, oW = o.JF, o.JF2, o.weights
+    in_range = oJF2 / nh * 4.0 ** -k >= 2.0 ** -80
+    assert oJF[~in_range].sum() < 1e-12 * oJF.sum()
+    eJF = np.abs(JF - oJF)[in_range] / oJF[in_range]
+    eJF2 = np.abs(JF2 - oJF2)[in_range] / oJF2[in_range]
+    big = oW >= 1e-20 * oW.max()
+    eW = np.abs(W - oW)[big] / oW[big]
+    qJF, qJF2, qW = _quantiles(eJF), _quantiles(eJF2), _quantiles(eW)
+    record_property("fp32_vs_fp64", {"JF": qJF, "JF2": qJF2, "weights": qW})
+    print("fp32 vs fp64 oracle", dim, n_it, pre, qJF, qJF2, qW)
+    assert qJF["p50"] <= 3e-4 and qJF["p999"] <= 3e-3 and qJF["max"] <= 0.5, qJF
+    assert qJF2["p50"] <= 6e-4 and qJF2["p999"] <= 6e-3 and qJF2["max"] <= 0.5, qJF2
+    assert qW["p50"] <= 3e-4 and qW["p99"] <= 5e-3 and qW["max"] <= 0.05, qW
+    assert np.abs(Cn.astype(np.int64) - o.counts).sum() <= 2e-4 * S * dim
+    assert abs(JF.sum() - oJF.sum()) <= 2e-6 * oJF.sum()
+
+
 def test_single_cube_and_fp32_against_fp64_oracle(ctx):
     """n_strat = 1 (d=12, 1e4 evals/iteration): one hypercube holds every sample;
     the reference maps this case on the CPU, here it stays on the GPU."""
