@@ -17,7 +17,8 @@ ABI_NATIVE, ABI_NUMBA = 0, 1
 FLAG_GRAPH, FLAG_NO_ADAPT, FLAG_TIME_FILL = 1, 2, 4
 STAGE_FILL, STAGE_REALLOC, STAGE_REFINE = 1, 2, 4
 (BUF_X_EDGES, BUF_NH, BUF_NH_SUM, BUF_JF, BUF_JF2, BUF_WEIGHTS, BUF_COUNTS, BUF_DH, BUF_THETA,
- BUF_ITERATION, BUF_UNIFORMS, BUF_STATS, BUF_SCALE_EXP, BUF_BIN_EXP, BUF_HIST_STATE) = range(15)
+ BUF_ITERATION, BUF_UNIFORMS, BUF_STATS, BUF_SCALE_EXP, BUF_BIN_EXP, BUF_HIST_STATE,
+ BUF_TILE_CUBE) = range(16)
 IT_CURRENT = 0xFFFFFFFF
 
 # every exported symbol of include/cuvegas.h

@@ -600,12 +600,22 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                     }
                     run = 0;
                 }
-                do {  // empty cubes (never produced by the reallocation) are skipped
-                    ++ci; ++c;
-                    cvg_cube_next<D, T>(ns, zs, zsh, coord, cdy);
-                    cstart = next;
-                    next = starts[ci + 1];
-                } while (l >= next && ci < K - 2);
+                if (ci < K - 2) {
+                    do {  // empty cubes (never produced by the reallocation) are skipped
+                        ++ci; ++c;
+                        cvg_cube_next<D, T>(ns, zs, zsh, coord, cdy);
+                        cstart = next;
+                        next = starts[ci + 1];
+                    } while (l >= next && ci < K - 2);
+                }
+                if (l >= next) {
+                    // the prefix ends before the tile map says (only after a
+                    // reallocation whose bounded wait ran out): report it and
+                    // stay in the tile's last cube, so every access stays in
+                    // bounds
+                    atomicOr(a.status, CVG_KSTAT_BAD_TILE);
+                    next = lend;
+                }
                 j = 0u;
             }
             ++run;

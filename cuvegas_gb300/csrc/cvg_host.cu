@@ -113,6 +113,8 @@ struct cvg_run_s {
     cvg_u32 *hist_state = nullptr;
     cvg_u64 *lb = nullptr;        // look-back words of the one-pass allocation
     cvg_u32 *lb_ctl = nullptr;
+    int lb_spin_limit = 0;        // CVG_LB_SPIN_LIMIT (0: the kernel's default, 2^22 polls)
+    cvg_u32 lb_withhold = 0;      // CVG_TEST_LB_WITHHOLD (failure test only; 0: none)
     cvg_u32 *tile_ctl = nullptr;  // the fill's warp-tile counter and CTA-done count
     cvg_u32 *done = nullptr;
     cvg_u64 *nh_sum = nullptr, *bsums = nullptr;
@@ -187,6 +189,16 @@ int env_warp_tiles()
     const char *e = std::getenv("CVG_FILL_WARP_TILES");
     if (!e || !*e) return -1;
     return e[0] == '0' ? 0 : 1;
+}
+
+// Non-negative integer from the environment, or `dflt` when unset or invalid.
+long env_long(const char *name, long dflt)
+{
+    const char *e = std::getenv(name);
+    if (!e || !*e) return dflt;
+    char *end = nullptr;
+    const long v = std::strtol(e, &end, 10);
+    return (end && *end == 0 && v >= 0) ? v : dflt;
 }
 
 // Integrand adaptor type F of the fill templates: static f (value) and df
@@ -442,6 +454,8 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.hist_min_it = 2;    // float bin sums in the fill after the first reallocation
     a.lb = r->lb;
     a.lb_ctl = r->lb_ctl;
+    a.lb_spin_limit = r->lb_spin_limit;
+    a.lb_withhold = r->lb_withhold;
     return a;
 }
 
@@ -590,10 +604,12 @@ cvg_status check_status(cvg_run_s *r)
     cvg_u32 st = 0;
     CK(cudaMemcpyAsync(&st, r->status, sizeof(st), cudaMemcpyDeviceToHost, r->ctx->stream));
     CK(cudaStreamSynchronize(r->ctx->stream));
-    if (st & CVG_KSTAT_BAD_TILE)
-        return fail(CVG_ERR_KERNEL, "fill kernel found an inconsistent tile map");
+    // a timed-out wait comes first: it leaves the prefix and tile map that
+    // the next fill then finds inconsistent
     if (st & CVG_KSTAT_TIMEOUT)
         return fail(CVG_ERR_KERNEL, "the reallocation's look-back wait ran out; results are not valid");
+    if (st & CVG_KSTAT_BAD_TILE)
+        return fail(CVG_ERR_KERNEL, "fill kernel found an inconsistent tile map");
     return CVG_OK;
 }
 
@@ -874,6 +890,13 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         return fail(CVG_ERR_INVALID, "evals per iteration + 2*n_cubes must stay below 2^31");
     }
     const int64_t nh0 = std::max<int64_t>(2, (int64_t)(1.0 / (double)r->n_cubes * (double)r->n_eval_it));
+
+    // bounded look-back wait of the one-pass allocation: CVG_LB_SPIN_LIMIT
+    // polls (default 2^22) before it gives up and reports CVG_ERR_KERNEL;
+    // CVG_TEST_LB_WITHHOLD = 1 + a chunk index makes that chunk never publish
+    // its word, so the failure test sees the wait run out (0 / unset: none)
+    r->lb_spin_limit = (int)std::min<long>(env_long("CVG_LB_SPIN_LIMIT", 0), 1L << 30);
+    r->lb_withhold = (cvg_u32)std::min<long>(env_long("CVG_TEST_LB_WITHHOLD", 0), 0xFFFFFFFFL);
 
     // tile shape
     const int wt_env = env_warp_tiles();
@@ -1183,6 +1206,7 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     case CVG_BUF_SCALE_EXP: src = r->scale_exp; need = sizeof(int); break;
     case CVG_BUF_BIN_EXP: src = r->bin_exp; need = sizeof(int) * ((size_t)D * N + 1); break;
     case CVG_BUF_HIST_STATE: src = r->hist_state; need = 2 * sizeof(cvg_u32); break;
+    case CVG_BUF_TILE_CUBE: src = r->tile_cube; need = sizeof(cvg_u32) * r->max_tiles; break;
     default: return fail(CVG_ERR_INVALID, "unknown buffer");
     }
     if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));

@@ -581,13 +581,16 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
     const cvg_u64 agg = block_exscan_u64(off, scratch);
 
     // decoupled look-back by warp 0, 32 predecessors at a time
+    const int spin_limit = a.lb_spin_limit > 0 ? a.lb_spin_limit : LB_SPIN_LIMIT;
+    const bool publish = blk + 1u != a.lb_withhold;   // false only in the failure test
     if (warp == 0) {
         cvg_u64 excl = 0;
         bool timeout = false;
         if (blk == 0) {
-            if (lane == 0) atomicExch((unsigned long long *)&a.lb[0], lb_word(epoch, LB_PRE, agg));
+            if (lane == 0 && publish) atomicExch((unsigned long long *)&a.lb[0], lb_word(epoch, LB_PRE, agg));
         } else {
-            if (lane == 0) atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_AGG, agg));
+            if (lane == 0 && publish)
+                atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_AGG, agg));
             int j = (int)blk - 1;
             while (true) {
                 const int idx = j - lane;
@@ -597,8 +600,8 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
                 do {
                     w = idx >= 0 ? *(volatile cvg_u64 *)&a.lb[idx] : lb_word(epoch, LB_PRE, 0);
                     ready = (cvg_u32)(w >> 34) == epoch;
-                } while (!__all_sync(0xffffffffu, ready) && ++spins < LB_SPIN_LIMIT);
-                if (spins >= LB_SPIN_LIMIT) { timeout = true; break; }
+                } while (!__all_sync(0xffffffffu, ready) && ++spins < spin_limit);
+                if (spins >= spin_limit) { timeout = true; break; }
                 const unsigned pm = __ballot_sync(0xffffffffu, (w & LB_PRE) != 0);
                 const int lp = pm ? __ffs(pm) - 1 : 31;
                 cvg_u64 v = lane <= lp ? (w & 0xFFFFFFFFull) : 0ull;
@@ -610,7 +613,8 @@ __global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
             }
             if (lane == 0) {
                 if (timeout) atomicOr(a.status, CVG_KSTAT_TIMEOUT);
-                atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_PRE, excl + agg));
+                if (publish)
+                    atomicExch((unsigned long long *)&a.lb[blk], lb_word(epoch, LB_PRE, excl + agg));
             }
         }
         if (lane == 0) s_excl = excl;
@@ -1145,8 +1149,48 @@ cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s)
     return cudaGetLastError();
 }
 
-cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a, const cvg_u32 *nh, cudaStream_t s)
+// Sum of JF2 over all hypercubes (FP64, one atomic per block); the last block
+// turns it into the FP32 reallocation's scale exponent: 2^(2k) ~ the mean of
+// (f*jac)^2 over the iteration's samples, as k3_finish_dev sets it after each
+// iteration of the loop.
+__global__ void __launch_bounds__(RB) k3_scale_from_sums(const double *JF2, const cvg_u64 *nh_sum,
+                                                        cvg_u32 n_cubes, double *ss,
+                                                        cvg_u32 *ticket, int *scale_exp)
 {
+    __shared__ double scratch[32];
+    double v[1] = {0.0};
+    for (cvg_u64 c = (cvg_u64)blockIdx.x * RB + threadIdx.x; c < n_cubes; c += (cvg_u64)gridDim.x * RB)
+        v[0] += JF2[c];
+    block_sum<1>(v, scratch);
+    if (threadIdx.x == 0) atomicAdd(ss, v[0]);
+    if (last_block(ticket, gridDim.x) && threadIdx.x == 0) {
+        const double S = (double)nh_sum[n_cubes];
+        const double ms = S > 0.0 ? *(volatile double *)ss / S : 0.0;
+        int k = 0;
+        if (ms > 0.0 && isfinite(ms)) {
+            int e = 0;
+            frexp(ms, &e);
+            k = e / 2;
+            k = k < -100 ? -100 : (k > 100 ? 100 : k);
+        }
+        *scale_exp = k;
+        *ss = 0.0;
+    }
+}
+
+cudaError_t cvg_launch_scale_from_sums(const double *JF2, const cvg_u64 *nh_sum, cvg_u32 n_cubes,
+                                       double *ss, cvg_u32 *ticket, int *scale_exp, cudaStream_t s)
+{
+    const unsigned nb = cvg_realloc_blocks(n_cubes);
+    k3_scale_from_sums<<<nb < 304u ? nb : 304u, RB, 0, s>>>(JF2, nh_sum, n_cubes, ss, ticket,
+                                                          scale_exp);
+    return cudaGetLastError();
+}
+
+cudaError_t cvg_launch_set_nh(const cvg_realloc_args &a_in, const cvg_u32 *nh, cudaStream_t s)
+{
+    cvg_realloc_args a = a_in;
+    a.lb_withhold = 0;   // the failure test's withheld word applies to reallocations only
     const unsigned nb = cvg_realloc_blocks(a.n_cubes);
     if (nh != a.nh_new) {
         cudaError_t e = cudaMemcpyAsync(a.nh_new, nh, sizeof(cvg_u32) * a.n_cubes,

@@ -56,6 +56,10 @@ struct cvg_realloc_args {
     cvg_u64 *lb;            // [n_blocks] look-back words of the one-pass allocation, or null
                             // (three-kernel path); zero before the first launch
     cvg_u32 *lb_ctl;        // [2]: block ticket (zero between launches), launch epoch
+    int lb_spin_limit;      // polls of a look-back word before the wait gives up and sets
+                            // CVG_KSTAT_TIMEOUT; 0 = the default (2^22)
+    cvg_u32 lb_withhold;    // failure test only: 1 + the chunk whose look-back word is never
+                            // published (its successors' waits then run out); 0 = none
 };
 
 struct cvg_refine_args {
@@ -95,6 +99,12 @@ __host__ __device__ inline unsigned cvg_realloc_blocks(cvg_u32 n_cubes)
 
 // Launch the reallocation chain (results, finish, count, scan, apply).
 cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s);
+// Scale exponent k of the FP32 reallocation from caller-given per-cube sums:
+// 2^k near the rms of f*jac, i.e. 2^(2k) ~ sum JF2 / total samples (the rule
+// k3_finish applies after every iteration).  ss (one double) and ticket (one
+// word) must be zero; both are left zero.
+cudaError_t cvg_launch_scale_from_sums(const double *JF2, const cvg_u64 *nh_sum, cvg_u32 n_cubes,
+                                       double *ss, cvg_u32 *ticket, int *scale_exp, cudaStream_t s);
 // Launch the refinement (one CTA per dimension).
 cudaError_t cvg_launch_refine(const cvg_refine_args &a, cudaStream_t s);
 // Tile map + prefix from an explicit nh (state import / initialisation).

@@ -16,7 +16,9 @@
 //  * all calls share the array: calls that overlap on the GPU (different
 //    streams, or host threads without ordering) race and corrupt each other;
 //  * the first call on a device looks up the array's device address with
-//    cudaGetSymbolAddress, so make that first call before any stream capture.
+//    cudaGetSymbolAddress, so make that first call before any stream capture;
+//  * each call waits for its kernels and reads their status word back, so it
+//    returns CVG_ERR_KERNEL when they found a non-finite estimate.
 #include "cuvegas.h"
 #include "cvg_kernels.cuh"
 
@@ -69,6 +71,12 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
         return reject(CVG_ERR_INVALID, "cvg_realloc_noalloc: bad precision");
     if (tile_cube && tile_samples < 1)
         return reject(CVG_ERR_INVALID, "cvg_realloc_noalloc: tile_samples must be >= 1");
+    // the fill's tile numbers and per-CTA sample claims are 32-bit: the same
+    // bound cvg_run_create applies
+    if (n_eval_it < 1 ||
+        (uint64_t)n_eval_it + 2ull * n_cubes >= (1ull << 31) - (1ull << 20))
+        return reject(CVG_ERR_INVALID, "cvg_realloc_noalloc: n_eval_it must be >= 1 and "
+                                       "n_eval_it + 2*n_cubes below 2^31 - 2^20");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
         return reject(CVG_ERR_CUDA, "cvg_realloc_noalloc: no current device");
@@ -98,7 +106,11 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
     a.acc = (cvg_acc_dev *)(b + kOffAcc);
     a.iteration = (cvg_u32 *)(b + kOffIt);
     a.status = (cvg_u32 *)(b + kOffStatus);
-    a.scale_exp = nullptr;               // JF/JF2 are taken at their own magnitude
+    // FP32 form: the per-cube sums are split into floats after scaling by
+    // 2^-k (JF) and 2^-2k (JF2), with 2^(2k) near the mean (f*jac)^2 of the
+    // iteration, worked out on the device from JF2 before the kernels run;
+    // the FP64 form takes the sums as they are
+    a.scale_exp = precision == CVG_PREC_FP32 ? (int *)(b + kOffIt + 144) : nullptr;
     a.done = (cvg_u32 *)(b + kOffIt + 64);   // block tickets (cleared below)
     a.stats = est;                       // est[0] = I, est[1] = sigma^2, est[2] = samples
     a.tile_cube = tile_cube;
@@ -115,7 +127,22 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
     // the array keeps the previous call's contents: clear what the kernels
     // accumulate into (sums, counters, status); the rest is overwritten
     cudaError_t e = cudaMemsetAsync(b + kOffAcc, 0, kOffStatus + 256 - kOffAcc, s);
+    if (e == cudaSuccess && a.scale_exp)
+        e = cvg_launch_scale_from_sums(JF2, a.nh_sum, n_cubes, (double *)(b + kOffIt + 128),
+                                       (cvg_u32 *)(b + kOffIt + 136), a.scale_exp, s);
     if (e == cudaSuccess) e = cvg_launch_realloc(a, s);
+    // the kernels report what they found in the array's status word: wait for
+    // them and read it (a 4-byte copy into this stack variable, no allocation)
+    cvg_u32 status = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&status, a.status, sizeof(status), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return reject(CVG_ERR_CUDA, cudaGetErrorString(e));
+    if (status & CVG_KSTAT_NONFINITE)
+        return reject(CVG_ERR_KERNEL, "cvg_realloc_noalloc: the iteration estimate or its "
+                                      "variance is not finite (non-finite JF/JF2 or overflow)");
+    if (status & (CVG_KSTAT_BAD_TILE | CVG_KSTAT_TIMEOUT))
+        return reject(CVG_ERR_KERNEL, "cvg_realloc_noalloc: the reallocation kernels reported "
+                                      "an inconsistent state (status " + std::to_string(status) + ")");
     return CVG_OK;
 }

@@ -154,7 +154,7 @@ _BUF_DTYPES = {
     L.BUF_JF: np.float64, L.BUF_JF2: np.float64, L.BUF_WEIGHTS: np.float64,
     L.BUF_COUNTS: np.uint32, L.BUF_DH: np.float64, L.BUF_THETA: np.float64,
     L.BUF_ITERATION: np.uint32, L.BUF_STATS: np.float64, L.BUF_SCALE_EXP: np.int32, L.BUF_BIN_EXP: np.int32,
-    L.BUF_HIST_STATE: np.uint32,
+    L.BUF_HIST_STATE: np.uint32, L.BUF_TILE_CUBE: np.uint32,
 }
 
 
@@ -220,7 +220,8 @@ class Run:
                 L.BUF_JF2: nc, L.BUF_WEIGHTS: D * N, L.BUF_COUNTS: D * N, L.BUF_DH: nc,
                 L.BUF_THETA: self.f.n_params, L.BUF_ITERATION: 1,
                 L.BUF_STATS: 3 * self.params.max_it, L.BUF_SCALE_EXP: 1,
-                L.BUF_BIN_EXP: D * N + 1, L.BUF_HIST_STATE: 2}[buf]
+                L.BUF_BIN_EXP: D * N + 1, L.BUF_HIST_STATE: 2,
+                L.BUF_TILE_CUBE: info.max_tiles}[buf]
 
     def get(self, buf):
         dt = _BUF_DTYPES[buf]

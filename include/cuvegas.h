@@ -176,9 +176,12 @@ enum {
                                 each bin's expected per-sample (f*jac)^2 for the next fill
                                 (unscaled; set by the pilot, then by each refinement); the
                                 last entry is the k of the last fill                      */
-    CVG_BUF_HIST_STATE = 14  /* uint32 [2]               get/set: FP32 form, [0] 1 = the next
+    CVG_BUF_HIST_STATE = 14, /* uint32 [2]               get/set: FP32 form, [0] 1 = the next
                                 fill keeps its bin sums in fixed point (chosen after each
                                 iteration from [1], the rare updates the fill counted)    */
+    CVG_BUF_TILE_CUBE = 15   /* uint32 [max_tiles]       get: the hypercube of each fill tile's
+                                first sample (tiles of tile_samples; entries past the next
+                                fill's last tile are stale)                                */
 };
 cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
 cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);
@@ -267,11 +270,17 @@ cvg_status cvg_batch_compile_check(const char *source, int32_t n_dims, const int
  * tile_samples; NULL skips it).  All temporaries live in one statically
  * allocated __device__ array (about 3 MiB per GPU that loads the library,
  * held until exit): n_cubes may not exceed CVG_NOALLOC_MAX_CUBES; larger
- * calls are rejected.  Calls share that array, so calls that overlap on the
- * GPU race.  The first call on a device looks up the array's address;
- * make that first call before any stream capture.  Calls no cudaMalloc or
- * cudaFree.  precision: CVG_PREC_FP64 (reference arithmetic) or
- * CVG_PREC_FP32 (compensated FP32 per cube).  stream may be NULL. */
+ * calls are rejected, and so are n_eval_it < 1 and n_eval_it + 2*n_cubes at
+ * or above 2^31 - 2^20 (the bound of cvg_run_create).  Calls share that
+ * array, so calls that overlap on the GPU race.  The first call on a device
+ * looks up the array's address; make that first call before any stream
+ * capture.  Calls no cudaMalloc or cudaFree.  precision: CVG_PREC_FP64
+ * (reference arithmetic) or CVG_PREC_FP32 (compensated FP32 per cube, on the
+ * sums scaled by a power of two worked out on the device from JF2, so sums of
+ * any magnitude in double range are taken).  The call waits for its kernels
+ * (it synchronises `stream`) and returns CVG_ERR_KERNEL when they report a
+ * non-finite estimate or variance, or an inconsistent state.  stream may be
+ * NULL. */
 #define CVG_NOALLOC_MAX_CUBES 262144
 cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_sum, uint32_t n_cubes,
                                double v_cubes, double beta, int64_t n_eval_it, int32_t precision,
