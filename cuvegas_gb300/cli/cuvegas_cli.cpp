@@ -300,7 +300,6 @@ int main(int argc, char **argv)
     }
 
     std::printf("GPUs: %d\n", 1);   // one GPU per process; replicas run as separate processes
-    const double t_ctx0 = now_ms();
     cvg_context ctx = nullptr;
     cvg_status st = cvg_context_create(device, nullptr, &ctx);
     if (st != CVG_OK) { std::fprintf(stderr, "cuvegas: %s\n", cvg_last_error()); return 1; }
@@ -312,6 +311,11 @@ int main(int argc, char **argv)
         cvg_context_destroy(ctx);
         return 1;
     }
+    // the reference compiles its integrand ahead of time (inlined into
+    // vegasFill at build time); here NVRTC compiles it now, and that time is
+    // reported on its own line so "Nocontext" keeps the reference's meaning:
+    // the run's own work after the device context exists
+    const double t_compiled = now_ms();
     cvg_result res{};
     st = cvg_integrate(ctx, f, &p, nullptr, &res, nullptr, nullptr);
     if (st != CVG_OK) {
@@ -329,8 +333,9 @@ int main(int argc, char **argv)
     std::printf("Total evals: %lld\n", (long long)res.tot_nevals);
     std::printf("Time elapsed %f ms\n", t_end - t_start);
     std::printf("Iteration avg time %f ms\n", res.avg_it_time_ms);
-    std::printf("Nocontext %f ms\n", t_end - t_nocontext);
-    std::printf("Context creation %f ms\n", t_nocontext - t_ctx0);
+    std::printf("Nocontext %f ms\n", t_end - t_compiled);
+    std::printf("Context creation %f ms\n", t_nocontext - t_start);
+    std::printf("Integrand compile %f ms\n", t_compiled - t_nocontext);
     std::printf("Chi2/dof: %f\n", res.chi2_dof);
     cvg_integrand_release(f);
     cvg_context_destroy(ctx);

@@ -9,11 +9,12 @@ import subprocess
 import pytest
 
 from cuvegas_gb300 import _build
+from oracle.ref_build import REF as REF_ROOT
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CFG = os.path.join(HERE, "golden", "cli", "config.cuh")
 SRC = os.path.join(HERE, "golden", "cli", "peaks.cu")
-REF = "/root/reference/src"     # the reference checkout, present only where it was surveyed
+REF = os.path.join(REF_ROOT, "src")     # the reference checkout, present only where it was surveyed
 
 
 def _cli(*args, timeout=600):
@@ -62,8 +63,14 @@ def test_cli_run_prints_reference_lines():
              for line in r.stdout.strip().splitlines()]
     assert [k for k, _ in pairs] == ["GPUs", "Strat", "Cubes", "Intervals", "Result", "Error",
                                      "Total evals", "Time elapsed", "Iteration avg time",
-                                     "Nocontext", "Context creation", "Chi2/dof"]
+                                     "Nocontext", "Context creation", "Integrand compile",
+                                     "Chi2/dof"]
     out = dict(pairs)
+    # the reference's meaning: Time elapsed = Context creation + Nocontext,
+    # with the JIT compile of the integrand (ahead of time in the reference)
+    # on its own line
+    parts = float(out["Context creation"]) + float(out["Integrand compile"]) + float(out["Nocontext"])
+    assert abs(float(out["Time elapsed"]) - parts) < 1.0
     exact = math.erf(5.0) ** 4
     res, err = float(out["Result"]), float(out["Error"])
     n_strat, n_cubes = int(out["Strat"]), int(out["Cubes"])
