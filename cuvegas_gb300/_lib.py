@@ -30,7 +30,7 @@ EXPORTS = (
     "cvg_run_last_fill_ms", "cvg_run_fill_times", "cvg_measure_peak", "cvg_realloc_noalloc",
     "cvg_batch_create", "cvg_batch_destroy", "cvg_batch_iterate", "cvg_batch_results",
     "cvg_batch_info_get", "cvg_batch_last_fill_ms", "cvg_batch_compile_check",
-    "cvg_context_trim", "cvg_compile_integrand_ptx",
+    "cvg_context_trim", "cvg_compile_integrand_ptx", "cvg_run_set_shard", "cvg_run_buffer",
 )
 NOALLOC_MAX_CUBES = 262144
 
@@ -108,6 +108,8 @@ def load():
             "cvg_run_sync": [vp],
             "cvg_run_get": [vp, C.c_int32, vp, sz],
             "cvg_run_set": [vp, C.c_int32, vp, sz],
+            "cvg_run_set_shard": [vp, C.c_int32, C.c_int32],
+            "cvg_run_buffer": [vp, C.c_int32, C.POINTER(vp), C.POINTER(sz)],
             "cvg_run_info_get": [vp, C.POINTER(RunInfo)],
             "cvg_run_grad": [vp, C.c_uint32, vp],
             "cvg_compile_check": [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,

@@ -66,6 +66,9 @@ struct cvg_fill_args {
     int tile_samples;             // samples per tile: 32 * spt (warp tiles) or blockDim.x * spt
     int spt;                      // consecutive samples per thread
     int n_params;
+    cvg_u32 shard;                // sample split across ranks: this fill covers tiles
+    cvg_u32 shards;               // [n_tiles*shard/shards, n_tiles*(shard+1)/shards) of the
+                                  // iteration (shards 0 or 1: all tiles)
     int pad0;
     double v_cubes;               // volume of one hypercube
     cvg_philox_keys keys;         // key schedule of seed

@@ -800,7 +800,7 @@ CVG_D bool cvg_fill_use_fixed(const cvg_fill_args &a)
 // budget (>= 152 CTAs) exceeds the 2^31 samples an iteration may hold.
 template <int D, typename T, int BS, bool ESM, bool HSM, bool REPLAY, int P, bool GRAD, class F,
           int NI, bool FIX>
-CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
+CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles, cvg_u64 t0, cvg_u64 t1)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
     constexpr int PP = P > 0 ? P : 1;
@@ -826,9 +826,10 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
         constexpr int W = BS / 32;
         if (tid == 0) claimed = (cvg_u32)(W * TS);
         __syncthreads();
-        // (tile numbers fit 32 bits: an iteration holds < 2^31 samples)
+        // (tile numbers fit 32 bits: an iteration holds < 2^31 samples);
+        // tiles are numbered from t0, the first tile of this fill's range
         const cvg_u32 lane = tid & 31;
-        const cvg_u32 n_warps = gridDim.x * W, nt = (cvg_u32)n_tiles;
+        const cvg_u32 n_warps = gridDim.x * W, nt = (cvg_u32)(t1 - t0);
         auto claim = [&]() -> cvg_u32 {
             cvg_u32 t = 0xFFFFFFFFu;
             if (lane == 0 && atomicAdd(&claimed, (cvg_u32)TS) + (cvg_u32)TS <= CVG_HIST_MAX_RUN)
@@ -840,13 +841,13 @@ CVG_D void cvg_fill_run(const cvg_fill_args &a, cvg_u64 S, cvg_u64 n_tiles)
         while (tile < nt) {
             const cvg_u32 next = n_warps < nt ? claim() : 0xFFFFFFFFu;
             if (!cvg_fill_tile<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, FIX, true>(
-                    a, sm, cx, tile, n_tiles, S, gacc, nrare, a.keys))
+                    a, sm, cx, t0 + tile, n_tiles, S, gacc, nrare, a.keys))
                 break;
             tile = next;
         }
     } else {
         cvg_u64 since = 0;   // samples in the shared histograms since their last flush
-        for (cvg_u64 tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        for (cvg_u64 tile = t0 + blockIdx.x; tile < t1; tile += gridDim.x) {
             if (since + (cvg_u64)TS > CVG_HIST_MAX_RUN) {
                 cvg_fill_flush<D, T, BS, ESM, HSM, P, GRAD, NI, FIX>(a, sm, true);
                 since = 0;
@@ -898,16 +899,22 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.status, CVG_KSTAT_BAD_TILE);
         n_tiles = a.max_tiles;
     }
+    // sample split across ranks: this fill's contiguous range of tiles
+    cvg_u64 t0 = 0, t1 = n_tiles;
+    if (a.shards > 1u) {
+        t0 = n_tiles * a.shard / a.shards;
+        t1 = n_tiles * (a.shard + 1u) / a.shards;
+    }
     // with warp tiles every CTA takes part (the last one to finish resets the
     // tile counter)
-    if (!CVG_FILL_WARP_TILES && (cvg_u64)blockIdx.x >= n_tiles) return;
+    if (!CVG_FILL_WARP_TILES && (cvg_u64)blockIdx.x >= t1 - t0) return;
     if constexpr (cvg_hist_fixed<D, T>() && HSM && !GRAD) {
         if (cvg_fill_use_fixed<D, T>(a))
-            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, true>(a, S, n_tiles);
+            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, true>(a, S, n_tiles, t0, t1);
         else
-            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles);
+            cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles, t0, t1);
     } else {
-        cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles);
+        cvg_fill_run<D, T, BS, ESM, HSM, REPLAY, P, GRAD, F, NI, false>(a, S, n_tiles, t0, t1);
     }
 }
 

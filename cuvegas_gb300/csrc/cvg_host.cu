@@ -113,6 +113,7 @@ struct cvg_run_s {
     cvg_u32 *hist_state = nullptr;
     cvg_u64 *lb = nullptr;        // look-back words of the one-pass allocation
     cvg_u32 *lb_ctl = nullptr;
+    cvg_u32 shard = 0, shards = 1;   // sample split: this run's fills cover one range of tiles
     int lb_spin_limit = 0;        // CVG_LB_SPIN_LIMIT (0: the kernel's default, 2^22 polls)
     cvg_u32 lb_withhold = 0;      // CVG_TEST_LB_WITHHOLD (failure test only; 0: none)
     cvg_u32 *tile_ctl = nullptr;  // the fill's warp-tile counter and CTA-done count
@@ -504,6 +505,8 @@ cvg_fill_args fill_args(cvg_run_s *r)
     a.tile_samples = r->TS;
     a.spt = r->spt;
     a.n_params = r->f->n_params;
+    a.shard = r->shard;
+    a.shards = r->shards;
     a.v_cubes = r->v_cubes;
     cvg_philox_schedule(r->p.seed, a.keys);
     return a;
@@ -512,6 +515,7 @@ cvg_fill_args fill_args(cvg_run_s *r)
 cvg_status launch_fill(cvg_run_s *r, const fill_variant &v, bool timed)
 {
     cvg_fill_args a = fill_args(r);
+    if (&v == &r->gradk) a.shards = 1;   // the gradient pass covers every sample
     void *args[] = {&a};
     const int grid = (int)std::min<cvg_u64>((cvg_u64)v.occ * r->ctx->n_sm, r->max_tiles);
     r->grid = std::max(grid, 1);
@@ -1212,6 +1216,37 @@ cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes)
     if (bytes != need) return fail(CVG_ERR_INVALID, "size mismatch: expected " + std::to_string(need));
     CK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, r->ctx->stream));
     CK(cudaStreamSynchronize(r->ctx->stream));
+    return CVG_OK;
+}
+
+cvg_status cvg_run_set_shard(cvg_run r, int32_t shard, int32_t shards)
+{
+    if (!r) return fail(CVG_ERR_INVALID, "NULL run");
+    if (shards < 1 || shard < 0 || shard >= shards)
+        return fail(CVG_ERR_INVALID, "shard must lie in [0, shards), shards >= 1");
+    if (r->graph_exec)
+        return fail(CVG_ERR_STATE, "set the shard before the first CUDA-graph iteration");
+    r->shard = (cvg_u32)shard;
+    r->shards = (cvg_u32)shards;
+    return CVG_OK;
+}
+
+cvg_status cvg_run_buffer(cvg_run r, int32_t buf, void **device_ptr, size_t *bytes)
+{
+    if (!r || !device_ptr || !bytes) return fail(CVG_ERR_INVALID, "NULL argument");
+    const int D = r->f->dim, N = r->p.n_intervals;
+    switch (buf) {
+    case CVG_BUF_X_EDGES: *device_ptr = r->x_edges; *bytes = sizeof(double) * D * (N + 1); break;
+    case CVG_BUF_NH_SUM: *device_ptr = r->nh_sum; *bytes = sizeof(cvg_u64) * ((size_t)r->n_cubes + 1); break;
+    case CVG_BUF_JF: *device_ptr = r->JF; *bytes = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_JF2: *device_ptr = r->JF2; *bytes = sizeof(double) * r->n_cubes; break;
+    case CVG_BUF_WEIGHTS: *device_ptr = r->weights; *bytes = sizeof(double) * D * N; break;
+    case CVG_BUF_COUNTS: *device_ptr = r->counts; *bytes = sizeof(cvg_u32) * D * N; break;
+    case CVG_BUF_HIST_STATE:
+        if (r->p.precision != CVG_PREC_FP32) return fail(CVG_ERR_INVALID, "FP64 runs keep no histogram state");
+        *device_ptr = r->hist_state; *bytes = 2 * sizeof(cvg_u32); break;
+    default: return fail(CVG_ERR_INVALID, "no device view of this buffer");
+    }
     return CVG_OK;
 }
 

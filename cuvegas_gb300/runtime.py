@@ -303,6 +303,18 @@ class Run:
         with np.load(path) as z:
             return {k: (z[k] if z[k].ndim else z[k].item()) for k in z.files}
 
+    # ---- sample split across ranks (cvg_run_set_shard / cvg_run_buffer) ----
+    def set_shard(self, shard, shards):
+        """Fill only tiles [T*shard/shards, T*(shard+1)/shards) of each
+        iteration (see cuvegas_gb300.shard)."""
+        L.check(self._lib.cvg_run_set_shard(self.handle, int(shard), int(shards)))
+
+    def buffer(self, buf):
+        """(device address, bytes) of one of the run's buffers."""
+        ptr, n = C.c_void_p(), C.c_size_t()
+        L.check(self._lib.cvg_run_buffer(self.handle, int(buf), C.byref(ptr), C.byref(n)))
+        return ptr.value, n.value
+
     def grad(self, it=L.IT_CURRENT):
         g = np.zeros(self.f.n_params)
         L.check(self._lib.cvg_run_grad(self.handle, int(it), g.ctypes.data_as(C.c_void_p)))

@@ -186,6 +186,31 @@ enum {
 cvg_status cvg_run_get(cvg_run r, int32_t buf, void *host, size_t bytes);
 cvg_status cvg_run_set(cvg_run r, int32_t buf, const void *host, size_t bytes);
 
+/* ---- sample split of one integral across ranks (one GPU per rank) ----
+ * Replaces the reference's multi-GPU iteration (src/main.cu:591-654 and
+ * vegas_cuda/src/vegas_cuda_extension/cuda_wrapper.cu:646-706): each GPU
+ * fills its share of the iteration's samples, the per-cube and per-bin sums
+ * are added across GPUs, and every GPU then holds the same sums.  Here each
+ * rank creates the same run (same parameters, seed and instance) and calls
+ * cvg_run_set_shard(r, rank, world): its fills then cover tiles
+ * [T*rank/world, T*(rank+1)/world) of the iteration's T tiles, a contiguous
+ * range of the samples in hypercube order.  The Philox counter names each
+ * sample by (sample-in-cube, cube, iteration), so the union of the ranks'
+ * fills is exactly the one-rank fill.  Per iteration: cvg_run_step(FILL);
+ * sum JF, JF2, WEIGHTS and COUNTS (and, in the FP32 form, HIST_STATE word
+ * [1]) over the ranks with any all-reduce (NCCL on the device views below,
+ * or host copies); cvg_run_step(REALLOC | REFINE), which every rank then
+ * computes identically (the reference broadcasts rank 0's grid instead,
+ * src/main.cu:531-541).  The gradient pass always covers every sample.
+ * Set the shard before the first graph iteration. */
+cvg_status cvg_run_set_shard(cvg_run r, int32_t shard, int32_t shards);
+/* Device address and size of one of the run's buffers (CVG_BUF_X_EDGES,
+ * NH_SUM, JF, JF2, WEIGHTS, COUNTS, HIST_STATE), for collectives issued by
+ * the caller on the context's stream.  The address stays valid until
+ * cvg_run_destroy.  No counterpart in the reference (its buffers are local
+ * to integrate_cuda). */
+cvg_status cvg_run_buffer(cvg_run r, int32_t buf, void **device_ptr, size_t *bytes);
+
 /* Sizes of the run: n_cubes, n_strat, samples of the next fill, tile shape. */
 typedef struct {
     int64_t n_eval_it, n_cubes, next_samples, max_tiles;
