@@ -226,66 +226,99 @@ CVG_D float cvg_pow2_16me(int e)
     asm("mad.lo.s32 %0, %1, -8388608, 1199570944;" : "=r"(b) : "r"(e));
     return __int_as_float(b);
 }
-// Fixed-point update of bin i without branches: returns 1 if w did not fit
-// (the caller adds it to the global FP64 sum), 2 if the word wrapped (the
-// caller adds 2^(16+e)), 0 otherwise (almost always).
-CVG_D cvg_u32 cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w)
+// Fixed-point update of bin i, with no branch and no select: adds
+// u = round(w * 2^(16-e)) units to the bin's word.  Two cases are rare and are
+// settled after all of a sample's updates, behind one branch (cvg_hist_rare):
+//  * the weight does not fit (w >= 2^(e+7), or not finite): its u is >= 2^23
+//    (for a non-finite w some large value); it is added all the same, OR-ed
+//    into `big`, and the rare step takes it back out of the word;
+//  * the word wraps: the carry out of the 32-bit add is shifted into `wraps`
+//    by a carry chain (wraps = 2*wraps + carry), so after a sample's D
+//    updates bit D-1-d says that dimension d's word wrapped (2^32 units more
+//    go to the global FP64 sum).
+// Every add and every take-back has its carry or borrow accounted for, so
+// the global sum plus the word's final value is exactly the sum of the
+// units that fitted: the same result as adding only those.  The rare step
+// recomputes u from the bin's exponent (the top byte of its count word,
+// fixed between flushes) by the same float operations.
+CVG_D void cvg_hist_add_fix(float *hw, cvg_u32 *hc, int i, float w, cvg_u32 &wraps, cvg_u32 &big)
 {
     const int e = (int)atomicAdd(hc + i, 1u) >> 24;          // this bin's scale exponent
     const float s = w * cvg_pow2_16me(e);                     // w * 2^(16-e)
-    const bool fits = s < 8388608.0f;
-    const cvg_u32 q = fits ? __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u : 0u;
-    const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, q);
-    return (fits ? 0u : 1u) | (o + q < o ? 2u : 0u);
+    const cvg_u32 u = __float_as_uint(__fadd_rn(s, 8388608.0f)) - 0x4B000000u;
+    const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i, u);
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %1, %2;\n\taddc.u32 %0, %0, %0;\n\t}"
+        : "+r"(wraps) : "r"(o), "r"(u));
+    big |= u;
 }
-// G updates (G even; bins i[0..G), one weight w): all count atomics first,
-// then the scale arithmetic in pairs, then the value atomics, so that G
-// shared-memory round trips overlap.  Leaves each update's rare code in
-// rare[] (as cvg_hist_add_fix).
+// G updates (G even; bins i[0..G), one weight w), as cvg_hist_add_fix: all
+// count atomics first, then the scale arithmetic in pairs, then the value
+// atomics, so that G shared-memory round trips overlap.
 template <int G>
-CVG_D void cvg_hist_group(float *hw, cvg_u32 *hc, const int *i, float w, cvg_u32 *rare)
+CVG_D void cvg_hist_group(float *hw, cvg_u32 *hc, const int *i, float w, cvg_u32 &wraps,
+                          cvg_u32 &big)
 {
     const float C = 8388608.0f;
     int e[G];
-    float s[G], q[G];
+    float q[G];
 #pragma unroll
     for (int k = 0; k < G; ++k) e[k] = (int)atomicAdd(hc + i[k], 1u) >> 24;
 #pragma unroll
     for (int k = 0; k < G; k += 2) {
         const cvg_f32x2 s2 = cvg_mul2(cvg_pack2(w, w),
                                       cvg_pack2(cvg_pow2_16me(e[k]), cvg_pow2_16me(e[k + 1])));
-        cvg_unpack2(s2, s[k], s[k + 1]);
         cvg_unpack2(cvg_add2(s2, cvg_pack2(C, C)), q[k], q[k + 1]);
     }
 #pragma unroll
     for (int k = 0; k < G; ++k) {
-        const bool f = s[k] < C;
-        const cvg_u32 u = f ? __float_as_uint(q[k]) - 0x4B000000u : 0u;
+        const cvg_u32 u = __float_as_uint(q[k]) - 0x4B000000u;
         const cvg_u32 o = atomicAdd(reinterpret_cast<cvg_u32 *>(hw) + i[k], u);
-        rare[k] = (f ? 0u : 1u) | (o + u < o ? 2u : 0u);
+        asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %1, %2;\n\taddc.u32 %0, %0, %0;\n\t}"
+            : "+r"(wraps) : "r"(o), "r"(u));
+        big |= u;
     }
 }
-CVG_D void cvg_hist_rare(const cvg_u32 *hc, double *gw, int i, cvg_u32 rare, float w)
-{
-    if (rare & 1u) atomicAdd(gw + i, cvg_f2d(w));
-    if (rare & 2u) atomicAdd(gw + i, __hiloint2double((1039 + ((int)hc[i] >> 24)) << 20, 0));
-}
 // Dimensions d0..d0+G-1 of one sample (bins bin[], weight w) through
-// cvg_hist_group; the rare codes returned as 2-bit fields at bit 2*(d0+k) of
-// a per-sample mask.
+// cvg_hist_group.
 template <int G>
-CVG_D cvg_u32 cvg_fill_hist_group_mask(float *hw, cvg_u32 *hc, double *gw, int d0, int N,
-                                       const int *bin, float w)
+CVG_D void cvg_fill_hist_group(float *hw, cvg_u32 *hc, int d0, int N, const int *bin, float w,
+                               cvg_u32 &wraps, cvg_u32 &big)
 {
     int i[G];
-    cvg_u32 rare[G];
 #pragma unroll
     for (int k = 0; k < G; ++k) i[k] = (d0 + k) * N + bin[d0 + k];
-    cvg_hist_group<G>(hw, hc, i, w, rare);
-    cvg_u32 m = 0;
-#pragma unroll
-    for (int k = 0; k < G; ++k) m |= rare[k] << (2 * (d0 + k));
-    return m;
+    cvg_hist_group<G>(hw, hc, i, w, wraps, big);
+}
+// The rare updates of one sample (see cvg_hist_add_fix): for each dimension
+// whose word wrapped, 2^32 units (2^(16+e)) go to the global FP64 sum; for
+// each whose units did not fit, the units are taken back out of the word
+// (a borrow takes 2^32 units back from the global sum) and the weight itself
+// goes to the global sum.  Returns the number of rare updates.
+template <int D>
+CVG_D cvg_u32 cvg_hist_rare(float *hw, const cvg_u32 *hc, double *gw, int N, const int *bin,
+                            float w, cvg_u32 wraps)
+{
+    cvg_u32 n = 0;
+#pragma unroll   // bin[] stays in registers (a loop indexing it would move it to the stack)
+    for (int d = 0; d < D; ++d) {
+        const int i = d * N + bin[d];
+        const int e = (int)hc[i] >> 24;
+        const double unit32 = __hiloint2double((1039 + e) << 20, 0);   // 2^32 units = 2^(16+e)
+        bool rare = false;
+        if ((wraps >> (D - 1 - d)) & 1u) {
+            atomicAdd(gw + i, unit32);
+            rare = true;
+        }
+        const cvg_u32 u = __float_as_uint(__fadd_rn(w * cvg_pow2_16me(e), 8388608.0f)) - 0x4B000000u;
+        if (u >= 0x800000u) {
+            const cvg_u32 o = atomicSub(reinterpret_cast<cvg_u32 *>(hw) + i, u);
+            if (o < u) atomicAdd(gw + i, -unit32);
+            atomicAdd(gw + i, cvg_f2d(w));
+            rare = true;
+        }
+        n += rare ? 1u : 0u;
+    }
+    return n;
 }
 // Bin sum and count of a shared-memory histogram entry, in the units of the
 // global histogram.
@@ -691,29 +724,24 @@ CVG_D bool cvg_fill_tile(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM, 
                     // dimensions are collected in a mask and handled behind
                     // one branch per sample.  Groups of CVG_HIST_GROUP, then
                     // of 4 and 2, then one dimension.
-                    static_assert(D <= 16, "2-bit rare codes of every dimension in 32 bits");
+                    static_assert(D <= 32, "one wrap bit per dimension in 32 bits");
                     constexpr int HG = CVG_HIST_GROUP;
                     constexpr int R0 = (D / HG) * HG;
                     constexpr int R1 = R0 + ((D - R0) / 4) * 4;
                     constexpr int R2 = R1 + ((D - R1) / 2) * 2;
-                    cvg_u32 m = 0;
+                    cvg_u32 wraps = 0u, big = 0u;   // in dimension order: see cvg_hist_add_fix
 #pragma unroll
                     for (int d0 = 0; d0 < R0; d0 += HG)
-                        m |= cvg_fill_hist_group_mask<HG>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                        cvg_fill_hist_group<HG>(sm.hw, sm.hc, d0, N, bin, jf2, wraps, big);
 #pragma unroll
                     for (int d0 = R0; d0 < R1; d0 += 4)
-                        m |= cvg_fill_hist_group_mask<4>(sm.hw, sm.hc, a.weights, d0, N, bin, jf2);
+                        cvg_fill_hist_group<4>(sm.hw, sm.hc, d0, N, bin, jf2, wraps, big);
                     if constexpr (R2 > R1)
-                        m |= cvg_fill_hist_group_mask<2>(sm.hw, sm.hc, a.weights, R1, N, bin, jf2);
+                        cvg_fill_hist_group<2>(sm.hw, sm.hc, R1, N, bin, jf2, wraps, big);
                     if constexpr (D > R2)
-                        m |= cvg_hist_add_fix(sm.hw, sm.hc, R2 * N + bin[R2], jf2) << (2 * R2);
-                    if (m) {
-#pragma unroll
-                        for (int d = 0; d < D; ++d) {
-                            const cvg_u32 r = (m >> (2 * d)) & 3u;
-                            if (r) { cvg_hist_rare(sm.hc, a.weights, d * N + bin[d], r, jf2); ++nrare; }
-                        }
-                    }
+                        cvg_hist_add_fix(sm.hw, sm.hc, R2 * N + bin[R2], jf2, wraps, big);
+                    if (wraps | (big >> 23))
+                        nrare += cvg_hist_rare<D>(sm.hw, sm.hc, a.weights, N, bin, jf2, wraps);
                 } else {
 #pragma unroll
                     for (int d = 0; d < D; ++d) {
