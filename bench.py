@@ -362,17 +362,26 @@ def tt_sweep(f, prec, exact, evals, iters=ITERS, skip=SKIP):
             "iterations": iters, "skip": skip, "points": pts}
 
 
-def run_timed(f, dim, n_it, iters, prec, stream, torch, theta=None, skip=SKIP, fill_times=True):
+def run_timed(f, dim, n_it, iters, prec, stream, torch, theta=None, skip=SKIP, fill_times=True,
+              nh_stats=False):
     """Iterations timed as CUDA-graph replays (CUDA events); fill launch
-    times from an eager run of the same workload (events around each fill)."""
+    times from an eager run of the same workload (events around each fill;
+    with nh_stats, also the sample counts of the largest hypercubes of that
+    run's last allocation)."""
+    import numpy as np
     from cuvegas_gb300 import _lib as L, runtime
-    fills = []
+    fills, nhs = [], None
     if fill_times:
         p = runtime.make_params(dim, n_it * iters, iters, skip=skip, n_intervals=NBINS, seed=SEED,
                                 precision=prec, flags=L.FLAG_TIME_FILL)
         with runtime.Run(f, p, theta) as r:
             r.iterate(iters)
             fills = list(r.fill_times()[1:])
+            if nh_stats:
+                nh = r.get(L.BUF_NH)
+                nhs = {"max": int(nh.max()), "cubes_ge_1e4": int((nh >= 10_000).sum()),
+                       "cubes_ge_1e6": int((nh >= 1_000_000).sum()),
+                       "share_of_samples_in_cubes_ge_1e4": float(nh[nh >= 10_000].sum() / nh.sum())}
     p = runtime.make_params(dim, n_it * iters, iters, skip=skip, n_intervals=NBINS, seed=SEED,
                             precision=prec, flags=L.FLAG_GRAPH)
     with runtime.Run(f, p, theta) as r:
@@ -385,7 +394,7 @@ def run_timed(f, dim, n_it, iters, prec, stream, torch, theta=None, skip=SKIP, f
         info = r.info
     ev = float(st[2, 1:iters].sum())
     return dict(res=res, it_res=it_res, it_sig=it_sig, it_ms=it_ms, fills=fills, evals=ev,
-                ms=float(sum(it_ms)), clk=clk.summary(), info=info)
+                ms=float(sum(it_ms)), clk=clk.summary(), info=info, nh_stats=nhs)
 
 
 def time_to_rel(it_res, it_sig, it_ms, skip, target=1e-4, exact=None):
@@ -420,36 +429,45 @@ def _form_summary(m, iters, exact, prec):
         fill_ms = float(np.mean(m["fills"]))
         d["fill_ms_mean"] = fill_ms
         d["realloc_refine_ms"] = step_ms - fill_ms
+    if m.get("nh_stats"):
+        d["fill_ms_per_iteration"] = [round(float(x), 4) for x in m["fills"]]
+        d["nh_largest_hypercubes"] = m["nh_stats"]
     return d
 
 
-def summary_c1(ctx, stream, torch, quick=False):
+def summary_c1(ctx, stream, torch, quick=False, evals=None):
     """C1: Gaussian d=4, 1e6 evals/iteration, 10 iterations, 1024 bins."""
     from cuvegas_gb300 import _lib as L, integrands as I, analytic as A
+    n_it = evals or 1_000_000
     f = ctx.integrand(I.GAUSS, 4)
     exact = A.gauss_normalised(4)
-    out = {"workload": "gauss-d4-1e6x10", "dim": 4, "evals_per_iteration": 1_000_000,
+    out = {"workload": "gauss-d4-%.0ex10" % n_it, "dim": 4, "evals_per_iteration": n_it,
            "iterations": 10}
     for name, prec in (("chosen", L.PREC_FP32), ("plain", L.PREC_FP64)):
-        m = run_timed(f, 4, 1_000_000, 10, prec, stream, torch)
+        m = run_timed(f, 4, n_it, 10, prec, stream, torch)
         out[name] = _form_summary(m, 10, exact, prec)
     out["speedup_chosen_vs_plain"] = out["chosen"]["value"] / out["plain"]["value"]
     return out
 
 
-def summary_c5(ctx, stream, torch, quick=False):
-    """C5: corner peak d=16, 1e9 evals/iteration, 20 iterations, 1024 bins."""
+def summary_c5(ctx, stream, torch, quick=False, evals=None):
+    """C5: corner peak d=16, 1e9 evals/iteration, 20 iterations, 1024 bins.
+    The chosen form also reports every iteration's fill time and the sample
+    counts of its largest hypercubes after adaptation (per-hypercube sums of
+    runs that share a hypercube go to FP64 atomics; a warp that lies wholly in
+    one hypercube combines its runs first)."""
     from cuvegas_gb300 import _lib as L, integrands as I, analytic as A
+    n_it = evals or 1_000_000_000
     th = I.corner_theta(0, 16)
     f = ctx.integrand(I.CORNER, 16, n_params=16)
     exact = A.corner_peak(th)
-    out = {"workload": "corner-d16-1e9x20", "dim": 16, "evals_per_iteration": 1_000_000_000,
+    out = {"workload": "corner-d16-%.0ex20" % n_it, "dim": 16, "evals_per_iteration": n_it,
            "iterations": 20}
-    m = run_timed(f, 16, 1_000_000_000, 20, L.PREC_FP32, stream, torch, th)
+    m = run_timed(f, 16, n_it, 20, L.PREC_FP32, stream, torch, th, nh_stats=True)
     out["chosen"] = _form_summary(m, 20, exact, L.PREC_FP32)
     if not quick:
         # plain: graph-replayed iterations only (no separate fill-timed run)
-        m = run_timed(f, 16, 1_000_000_000, 20, L.PREC_FP64, stream, torch, th, fill_times=False)
+        m = run_timed(f, 16, n_it, 20, L.PREC_FP64, stream, torch, th, fill_times=False)
         out["plain"] = _form_summary(m, 20, exact, L.PREC_FP64)
         out["speedup_chosen_vs_plain"] = out["chosen"]["value"] / out["plain"]["value"]
     return out
@@ -799,7 +817,8 @@ def run_workload(args):
     ctx = runtime.Context(0, stream=C_stream(stream))
     fn = {"c1": summary_c1, "c3": summary_c3, "c4": summary_c4, "c5": summary_c5}[args.workload]
     out = {"n_gpus": 1, "data": "synthetic"}
-    out.update(fn(ctx, stream, torch, quick=args.quick))
+    kw = {"evals": args.evals} if args.workload in ("c1", "c5") and args.evals else {}
+    out.update(fn(ctx, stream, torch, quick=args.quick, **kw))
     if args.workload == "c1" and not args.no_cpu:
         import numpy as np
         from oracle import pyoracle as Po

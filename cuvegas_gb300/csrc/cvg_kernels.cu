@@ -513,8 +513,10 @@ __device__ __forceinline__ cvg_u64 lb_word(cvg_u32 epoch, cvg_u64 flag, cvg_u64 
 // Epochs run 1 .. 2^30 - 1 (0 marks a word never written).
 __device__ __forceinline__ cvg_u32 lb_next_epoch(cvg_u32 e) { return e % 0x3FFFFFFFu + 1u; }
 
+// 8 CTAs per SM (32 registers; a few bytes spill): more blocks in their
+// look-back at once (C2: 76.9 -> 69.6 us against 6 CTAs at 40 registers)
 template <int MODE>
-__global__ void __launch_bounds__(RB) k3_alloc(cvg_realloc_args a, unsigned nb)
+__global__ void __launch_bounds__(RB, 8) k3_alloc(cvg_realloc_args a, unsigned nb)
 {
     __shared__ cvg_u64 scratch[33];
     __shared__ unsigned s_blk;
