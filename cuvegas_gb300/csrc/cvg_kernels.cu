@@ -664,11 +664,11 @@ constexpr int CL = 8;      // CTAs per cluster (portable size)
 constexpr int KB = 128;    // threads per CTA
 
 // Dynamic shared memory of one K4 CTA: doubles w[B+2] sw[B] cs[B] fsw[N]
-// fcs[N] xo[N+1] fw[N], then ints fdv[N] eb[B].
+// fcs[N] xo[N+1] fw[N], then ints fdv[N] eb[B] dv[B].
 __host__ __device__ inline size_t k4_smem_bytes(int N)
 {
     const size_t B = (size_t)((N + CL - 1) / CL);
-    return sizeof(double) * (3 * B + 4 * (size_t)N + 3) + sizeof(int) * ((size_t)N + B) + 16;
+    return sizeof(double) * (3 * B + 4 * (size_t)N + 3) + sizeof(int) * ((size_t)N + 2 * B) + 16;
 }
 
 // Binary exponent of a positive finite double (denormals: -1023), else INT_MIN.
@@ -697,10 +697,11 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
     const int N = a.n_intervals, tid = threadIdx.x;
     const int B = (N + CL - 1) / CL;
     const int i0 = min(N, r * B), i1 = min(N, i0 + B), nb = i1 - i0;
-    // smem: w[B+2] (with halo) | sw[B] | cs[B] | fsw[N] | fcs[N] | xo[N+1] | fw[N] | fdv[N] | eb[B]
+    // smem: w[B+2] (with halo) | sw[B] | cs[B] | fsw[N] | fcs[N] | xo[N+1] | fw[N] | fdv[N] |
+    // eb[B] | dv[B]
     double *w = ks, *sw = w + B + 2, *cs = sw + B, *fsw = cs + B, *fcs = fsw + N, *xo = fcs + N;
     double *fw = xo + N + 1;
-    int *fdv = (int *)(fw + N), *eb = fdv + N;
+    int *fdv = (int *)(fw + N), *eb = fdv + N, *dv = eb + B;
     // FP32 form: per-bin exponents of the expected per-sample (f*jac)^2 of the
     // next fill (see the fill's histogram update); eb holds this CTA's bins
     const bool ex = a.bin_exp != nullptr;
@@ -751,7 +752,13 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
             if (i == 0) t = (7.0 * wc + wp) / (8.0 * dsum);
             else if (i == N - 1) t = (wm + 7.0 * wc) / (8.0 * dsum);
             else t = (wm + 6.0 * wc + wp) / (8.0 * dsum);
-            if (t != 0) t = pow((t - 1.0) / log(t), a.alpha);
+            if (t != 0) {
+                // ((t-1)/ln t)^alpha; alpha = 0.5 (the default) as a square
+                // root, correctly rounded and several times cheaper than pow
+                // on this GPU's FP64 pipe
+                const double v = (t - 1.0) / log(t);
+                t = a.alpha == 0.5 ? sqrt(v) : pow(v, a.alpha);
+            }
             sw[i - i0] = t;
             p2 += t;
         }
@@ -782,7 +789,14 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
         double pre = 0.0;
         for (int q = 0; q < r; ++q) pre += *cl.map_shared_rank(&part[2], q);
         ok = ssum > 0.0 && isfinite(ssum);
-        for (int j = tid; j < nb; j += KB) cs[j] += pre;
+        const double delta = ssum / N;
+        // the cumulative sum and setMap's div (src/main.cu:189-209) of this
+        // CTA's own bins; the cluster gathers both below (one FP64 division
+        // per bin in the cluster, not per bin in every CTA)
+        for (int j = tid; j < nb; j += KB) {
+            cs[j] += pre;
+            if (ok) dv[j] = (int)(cs[j] / delta);
+        }
         cl.sync();
         if (ok) {
             // gather sw and the scan of every bin of this dimension
@@ -790,15 +804,14 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
                 const int q0 = min(N, q * B), q1 = min(N, q0 + B);
                 const double *rsw = cl.map_shared_rank(sw, q), *rcs = cl.map_shared_rank(cs, q);
                 const double *rw = cl.map_shared_rank(w, q);
+                const int *rdv = cl.map_shared_rank(dv, q);
                 for (int j = tid; j < q1 - q0; j += KB) {
                     fsw[q0 + j] = rsw[j];
                     fcs[q0 + j] = rcs[j];
+                    fdv[q0 + j] = rdv[j];
                     if (ex) fw[q0 + j] = rw[j + 1];
                 }
             }
-            __syncthreads();
-            const double delta = ssum / N;
-            for (int i = tid; i < N; i += KB) fdv[i] = (int)(fcs[i] / delta);   // setMap div
             __syncthreads();
             // updateXEdges (src/main.cu:211-230): new edge k+1 lies in old
             // interval o = min{ i : div_i > k }, the interval setMap assigns to k
