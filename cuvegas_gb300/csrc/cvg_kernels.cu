@@ -307,50 +307,59 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
     }
     block_sum<4>(v, scratch);
     if (threadIdx.x == 0) {
+        // every load of the loop state first, then the arithmetic, then the
+        // stores: one round trip to memory instead of one per field (this step
+        // is on the critical path of small iterations)
+        cvg_acc_dev *acc = a.acc;
         const cvg_u32 it = *a.iteration;
+        const int kx = (a.fast_pow && a.scale_exp) ? *a.scale_exp : 0;
+        const cvg_u64 S = a.nh_sum[a.n_cubes];
+        const double sw = acc->sw, swr = acc->swr, swr2 = acc->swr2;
+        const cvg_u64 used = acc->used, tot = acc->tot_nevals;
+        const cvg_u32 rare_n = a.hist_state ? a.hist_state[1] : 0u;
+
         double r = v[1], s = v[2];
+        int knew = kx;
         if (a.fast_pow) {   // FP32 form sums m 2^-k and var 2^-2k / n without the cube volume
-            const int kx = a.scale_exp ? *a.scale_exp : 0;
             r = ldexp(r, kx) * a.v_cubes;
             s = ldexp(s, 2 * kx) * (a.v_cubes * a.v_cubes);
             if (a.scale_exp) {   // next scale: 2^k ~ rms of f*jac
-                const double ms = v[3] / (double)a.nh_sum[a.n_cubes];
+                const double ms = v[3] / (double)S;
                 if (ms > 0.0 && isfinite(ms)) {
                     int e = 0;
                     frexp(ms, &e);
-                    int knew = kx + e / 2;
+                    knew = kx + e / 2;
                     knew = knew < -100 ? -100 : (knew > 100 ? 100 : knew);
-                    *a.scale_exp = knew;
                 }
             }
         }
+        const bool in_mean = (int)it >= a.skip;   // src/main.cu:680, 698-713
+        // FP32 form: fixed-point bin sums in the next fill only from the third
+        // iteration on (the first reallocation of a peaked integrand moves
+        // the samples far from what the exponent table predicts) and only
+        // while rare updates stayed below 1 in 1024
+        const bool fixed_next = (int)it + 1 >= a.hist_min_it &&
+                                ldexp((double)rare_n, a.rare_shift) <= (double)S * (double)a.dim;
+
+        if (a.fast_pow && a.scale_exp) *a.scale_exp = knew;
         if ((int)it < a.max_it) {
             a.stats[it] = r;
             a.stats[a.max_it + it] = s;
-            a.stats[2 * a.max_it + it] = (double)a.nh_sum[a.n_cubes];
+            a.stats[2 * a.max_it + it] = (double)S;
         }
-        cvg_acc_dev *acc = a.acc;
         acc->dh_sum = v[0];
         acc->nh_scale = (double)a.n_eval_it / v[0];
-        const cvg_u64 S = a.nh_sum[a.n_cubes];
-        acc->tot_nevals += S;
+        acc->tot_nevals = tot + S;
         acc->last_nevals = S;
-        if ((int)it >= a.skip) {   // src/main.cu:680, 698-713
-            acc->sw += 1.0 / s;
-            acc->swr += r / s;
-            acc->swr2 += r * r / s;
-            acc->used += 1;
+        if (in_mean) {
+            acc->sw = sw + 1.0 / s;
+            acc->swr = swr + r / s;
+            acc->swr2 = swr2 + r * r / s;
+            acc->used = used + 1;
         }
         if (!isfinite(r) || !isfinite(s)) atomicOr(a.status, CVG_KSTAT_NONFINITE);
         if (a.hist_state) {
-            // FP32 form: fixed-point bin sums in the next fill only from the third
-            // iteration on (the first reallocation of a peaked integrand moves
-            // the samples far from what the exponent table predicts) and only
-            // while rare updates stayed below 1 in 1024
-            const double rare = (double)a.hist_state[1];
-            const bool ok = (int)it + 1 >= a.hist_min_it &&
-                            ldexp(rare, a.rare_shift) <= (double)S * (double)a.dim;
-            a.hist_state[0] = ok ? 1u : 0u;
+            a.hist_state[0] = fixed_next ? 1u : 0u;
             a.hist_state[1] = 0u;
         }
         *a.iteration = it + 1;
