@@ -586,9 +586,14 @@ cvg_status enqueue_stages(cvg_run_s *r, int stages, bool timed)
             CKS(launch_fill(r, r->fill, timed));
         }
     }
-    if ((stages & CVG_STAGE_REFINE) && (stages & CVG_STAGE_REALLOC)) {
+    if ((stages & CVG_STAGE_REFINE) && (stages & CVG_STAGE_REALLOC) &&
+        r->p.precision == CVG_PREC_FP32) {
         // independent: the grid refinement (few CTAs, latency bound) overlaps the
-        // reallocation (HBM bound); joined before the next fill
+        // reallocation (HBM bound); joined before the next fill.  FP32 form
+        // only: beside the FP64 form's reallocation, itself bound by this GPU's
+        // FP64 pipe, the refinement's clusters share its SMs and the iteration
+        // slows (graph replay, d=4, 1e6 evaluations: 0.88 ms forked, 0.38 ms
+        // in sequence; FP32 form 0.051 ms forked, 0.064 ms in sequence)
         cudaStream_t aux = r->ctx->aux;
         CK(cudaEventRecord(r->ev_fork, s));
         CK(cudaStreamWaitEvent(aux, r->ev_fork, 0));
