@@ -455,6 +455,7 @@ cvg_realloc_args realloc_args(cvg_run_s *r)
     a.hist_min_it = 2;    // float bin sums in the fill after the first reallocation
     a.lb = r->lb;
     a.lb_ctl = r->lb_ctl;
+    a.small_chunks = 1;
     a.lb_spin_limit = r->lb_spin_limit;
     a.lb_withhold = r->lb_withhold;
     return a;
@@ -979,7 +980,7 @@ cvg_status cvg_run_create(cvg_context ctx, cvg_integrand f, const cvg_params *pp
         {(void **)&r->nh_sum, sizeof(cvg_u64) * ((size_t)r->n_cubes + 1)},
         {(void **)&r->nh_new, sizeof(cvg_u32) * r->n_cubes},
         {(void **)&r->tile_cube, sizeof(cvg_u32) * r->max_tiles},
-        {(void **)&r->partials, sizeof(double) * 4 * r->nb},
+        {(void **)&r->partials, sizeof(double) * 4 * 4 * r->nb},   // small_chunks: 4x blocks
         {(void **)&r->bsums, sizeof(cvg_u64) * (r->nb + 1)},
         {(void **)&r->stats, sizeof(double) * 3 * p.max_it},
         {(void **)&r->acc, sizeof(cvg_acc_dev)},

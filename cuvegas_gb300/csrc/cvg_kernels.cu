@@ -145,13 +145,16 @@ __device__ __forceinline__ bool last_block(cvg_u32 *ctr, unsigned nb)
     return last;
 }
 
+// R hypercubes per thread (RIPT, or 2 for runs with few hypercubes, where
+// the per-thread chain of 8 would leave the launch latency-bound)
+template <int R = RIPT>
 __device__ __forceinline__ void k3_results_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double scratch[3 * 32];
-    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * (cvg_u32)(RB * R);
     double v[3] = {0.0, 0.0, 0.0};   // dh, I, sigma2
     const double vc = a.v_cubes;
-    for (int k = 0; k < RIPT; ++k) {
+    for (int k = 0; k < R; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
         const int neval = (int)(a.nh_sum[c + 1] - a.nh_sum[c]);
@@ -181,11 +184,11 @@ __device__ __forceinline__ void k3_results_dev(const cvg_realloc_args &a, const 
 __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb);
 __device__ void k3_scan_dev(const cvg_realloc_args &a, unsigned nb);
 
+template <int R>
 __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
 {
-    k3_results_dev(a, blockIdx.x);
-    const unsigned nb = cvg_realloc_blocks(a.n_cubes);
-    if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
+    k3_results_dev<R>(a, blockIdx.x);
+    if (last_block(&a.done[0], gridDim.x)) k3_finish_dev(a, gridDim.x);
 }
 
 
@@ -194,10 +197,11 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
 // d_h = (q - m^2)^beta (the constant V^(2 beta) cancels in the allocation).
 // Sums are compensated in FP32 per thread, FP64 across warps and blocks;
 // k3_finish multiplies by V and V^2.
+template <int R = RIPT>
 __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double wsum[4][RB / 32];
-    const cvg_u32 base = blk * CVG_REALLOC_CHUNK;
+    const cvg_u32 base = blk * (cvg_u32)(RB * R);
     const float beta = (float)a.beta;
     const int kx = a.scale_exp ? *a.scale_exp : 0;   // work on JF*2^-k, JF2*2^-2k
     dfloat sm = {0.f, 0.f};
@@ -208,10 +212,10 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
     double *__restrict__ JF2 = a.JF2;
     float *__restrict__ DH = reinterpret_cast<float *>(a.dh);   // FP32 form: d_h as float
     // issue every load of this thread's cubes before any store
-    cvg_u64 s0[RIPT], s1[RIPT];
-    double j1[RIPT], j2[RIPT];
+    cvg_u64 s0[R], s1[R];
+    double j1[R], j2[R];
 #pragma unroll
-    for (int k = 0; k < RIPT; ++k) {
+    for (int k = 0; k < R; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         const bool in = c < a.n_cubes;
         s0[k] = in ? nhs[c] : 0ull;
@@ -220,7 +224,7 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
         j2[k] = in ? JF2[c] : 0.0;
     }
 #pragma unroll
-    for (int k = 0; k < RIPT; ++k) {
+    for (int k = 0; k < R; ++k) {
         const cvg_u32 c = base + k * RB + threadIdx.x;
         if (c >= a.n_cubes) break;
         JF[c] = 0.0;
@@ -287,11 +291,11 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
 
 // 4 blocks per SM (64 registers, no spills): more loads in flight than the
 // 76-register build's 3 (C2 step 1.955 -> 1.938 ms); 5 or more spill
+template <int R>
 __global__ void __launch_bounds__(RB, 4) k3_results_f32(cvg_realloc_args a)
 {
-    k3_results_f32_dev(a, blockIdx.x);
-    const unsigned nb = cvg_realloc_blocks(a.n_cubes);
-    if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
+    k3_results_f32_dev<R>(a, blockIdx.x);
+    if (last_block(&a.done[0], gridDim.x)) k3_finish_dev(a, gridDim.x);
 }
 
 
@@ -1159,8 +1163,18 @@ cudaError_t cvg_launch_copy_bench(const float4 *src, float4 *dst, size_t n, cuda
 cudaError_t cvg_launch_realloc(const cvg_realloc_args &a, cudaStream_t s)
 {
     const unsigned nb = cvg_realloc_blocks(a.n_cubes);
-    if (a.fast_pow) k3_results_f32<<<nb, RB, 0, s>>>(a);   // + finish in the last block
-    else k3_results<<<nb, RB, 0, s>>>(a);
+    // + finish in the last block.  Runs with few hypercubes take 2 per thread
+    // (4x the blocks): the results kernel is then latency-bound, not
+    // bandwidth-bound (d=4, 1e6 evaluations, 234k hypercubes)
+    if (a.small_chunks && a.n_cubes <= CVG_REALLOC_SMALL_CUBES) {
+        const unsigned nb2 = (a.n_cubes + RB * 2 - 1) / (RB * 2);
+        if (a.fast_pow) k3_results_f32<2><<<nb2, RB, 0, s>>>(a);
+        else k3_results<2><<<nb2, RB, 0, s>>>(a);
+    } else if (a.fast_pow) {
+        k3_results_f32<RIPT><<<nb, RB, 0, s>>>(a);
+    } else {
+        k3_results<RIPT><<<nb, RB, 0, s>>>(a);
+    }
     if (a.adapt) {
         if (a.lb) {   // one pass: count, scan and apply
             if (a.fast_pow) k3_alloc<2><<<nb, RB, 0, s>>>(a, nb);

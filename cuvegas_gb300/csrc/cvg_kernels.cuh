@@ -56,6 +56,8 @@ struct cvg_realloc_args {
     cvg_u64 *lb;            // [n_blocks] look-back words of the one-pass allocation, or null
                             // (three-kernel path); zero before the first launch
     cvg_u32 *lb_ctl;        // [2]: block ticket (zero between launches), launch epoch
+    int small_chunks;       // 1: up to CVG_REALLOC_SMALL_CUBES hypercubes, the results kernel
+                            // takes 2 per thread (partials must hold 4x the blocks)
     int lb_spin_limit;      // polls of a look-back word before the wait gives up and sets
                             // CVG_KSTAT_TIMEOUT; 0 = the default (2^22)
     cvg_u32 lb_withhold;    // failure test only: 1 + the chunk whose look-back word is never
@@ -75,7 +77,8 @@ struct cvg_refine_args {
     int adapt;              // 0: only clear the histograms
 };
 
-enum { CVG_REALLOC_CHUNK = 2048, CVG_REFINE_BLOCK = 1024, CVG_REFINE_MAX_N = 4096 };
+enum { CVG_REALLOC_CHUNK = 2048, CVG_REFINE_BLOCK = 1024, CVG_REFINE_MAX_N = 4096,
+       CVG_REALLOC_SMALL_CUBES = 1 << 19 };
 
 // Device tables of a batch of instances (one launch covers all of them).
 struct cvg_realloc_batch {

@@ -37,7 +37,9 @@ constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kOffDh = 0;
 constexpr size_t kOffNh = kOffDh + align256(sizeof(double) * kMaxCubes);
 constexpr size_t kOffPart = kOffNh + align256(sizeof(cvg_u32) * kMaxCubes);
-constexpr size_t kOffBsum = kOffPart + align256(sizeof(double) * 4 * kMaxBlocks);
+// partials of the results kernel: 4 per block, with 4x the blocks at this
+// size (2 hypercubes per thread, as the loop's reallocation uses)
+constexpr size_t kOffBsum = kOffPart + align256(sizeof(double) * 4 * 4 * kMaxBlocks);
 constexpr size_t kOffAcc = kOffBsum + align256(sizeof(cvg_u64) * (kMaxBlocks + 1));
 constexpr size_t kOffIt = kOffAcc + align256(sizeof(cvg_acc_dev));
 constexpr size_t kOffStatus = kOffIt + 256;
@@ -124,6 +126,7 @@ extern "C" cvg_status cvg_realloc_noalloc(double *JF, double *JF2, uint64_t *nh_
     a.max_it = 1;
     a.fast_pow = precision == CVG_PREC_FP32 ? 1 : 0;
     a.adapt = 1;
+    a.small_chunks = 1;   // the same per-thread grouping as the loop at this size
     // the array keeps the previous call's contents: clear what the kernels
     // accumulate into (sums, counters, status); the rest is overwritten
     cudaError_t e = cudaMemsetAsync(b + kOffAcc, 0, kOffStatus + 256 - kOffAcc, s);
