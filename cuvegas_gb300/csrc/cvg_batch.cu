@@ -77,7 +77,10 @@ struct cvg_batch_s {
     cvg_refine_args *d_refine = nullptr;
     int *d_dims = nullptr;
     unsigned *d_blk_base = nullptr, *d_dim_base = nullptr;
-    cvg_u64 *d_tile_base = nullptr;
+    cvg_u64 *d_tile_base = nullptr, *d_cost_base = nullptr;
+    cvg_u64 *d_range_start = nullptr, *d_claim = nullptr;
+    cvg_u32 *d_range_inst = nullptr;
+    int max_ranges = 0;               // capacity of the range tables (32 CTAs per SM)
     cvg_u32 *d_status = nullptr;
     unsigned total_blocks = 0, total_dims = 0;
     cudaKernel_t fill = nullptr, pilot = nullptr;
@@ -137,6 +140,11 @@ void tables_layout(cvg_batch_s *b, char *base, size_t &off)
     place(b->d_blk_base, sizeof(unsigned) * (n + 1), base, off);
     place(b->d_dim_base, sizeof(unsigned) * (n + 1), base, off);
     place(b->d_tile_base, sizeof(cvg_u64) * (n + 1), base, off);
+    place(b->d_cost_base, sizeof(cvg_u64) * (n + 1), base, off);
+    const size_t R = (size_t)b->max_ranges;
+    place(b->d_range_start, sizeof(cvg_u64) * (R + 1), base, off);
+    place(b->d_range_inst, sizeof(cvg_u32) * R, base, off);
+    place(b->d_claim, sizeof(cvg_u64) * R, base, off);
 }
 
 std::string batch_source(const cvg_batch_s &b, const std::set<int> &dims)
@@ -186,7 +194,11 @@ cvg_batch_args batch_args(const cvg_batch_s *b)
     a.inst = b->d_fill;
     a.dims = b->d_dims;
     a.tile_base = b->d_tile_base;
+    a.range_start = b->d_range_start;
+    a.range_inst = b->d_range_inst;
+    a.claim = b->d_claim;
     a.n_inst = b->n;
+    a.n_ranges = b->grid;
     cvg_philox_schedule(b->p.seed, a.keys);
     return a;
 }
@@ -199,6 +211,18 @@ cvg_realloc_batch realloc_batch(const cvg_batch_s *b)
     B.total_blocks = b->total_blocks;
     B.n = b->n;
     return B;
+}
+
+cvg_batch_sched batch_sched(const cvg_batch_s *b)
+{
+    cvg_batch_sched S{};
+    S.tile_base = b->d_tile_base;
+    S.cost_base = b->d_cost_base;
+    S.range_start = b->d_range_start;
+    S.range_inst = b->d_range_inst;
+    S.claim = b->d_claim;
+    S.n_ranges = b->grid;
+    return S;
 }
 
 cvg_refine_batch refine_batch(const cvg_batch_s *b)
@@ -226,7 +250,7 @@ cvg_status enqueue_iteration(cvg_batch_s *b, bool timed)
     BCK(cvg_launch_refine_batch(refine_batch(b), b->p.n_intervals, aux));
     BCK(cudaEventRecord(b->ev_join, aux));
     BCK(cvg_launch_realloc_batch(realloc_batch(b), (b->p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1,
-                                 b->p.precision == CVG_PREC_FP32, b->d_tile_base, s));
+                                 b->p.precision == CVG_PREC_FP32, batch_sched(b), s));
     BCK(cudaStreamWaitEvent(s, b->ev_join, 0));
     return CVG_OK;
 }
@@ -267,6 +291,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         return cvg_internal_fail(CVG_ERR_INVALID, "bad block / spt");
     }
     b->TS = b->block * b->spt;
+    b->max_ranges = 32 * std::max(1, ctx->n_sm);
     const int N = p.n_intervals;
     std::set<int> dims;
     int dmax = 0, pmax = 0;
@@ -304,7 +329,8 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     tables_layout(b, nullptr, total);
     const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8;
     b->fill_smem = cvg_fill_smem_bytes(dmax, N, tsz, 1, 1, 0, b->TS, pmax, b->block);
-    if (b->fill_smem > (size_t)ctx->smem_optin) {
+    // (+ the fill's few static bytes: its claim slots)
+    if (b->fill_smem + 64 > (size_t)ctx->smem_optin) {
         delete b;
         return cvg_internal_fail(CVG_ERR_INVALID, "batch: grid and histograms of the largest "
                                                   "dimension do not fit shared memory");
@@ -444,8 +470,6 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
     BCK(cudaMemcpyAsync(b->d_dims, hdims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_blk_base, blk_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_dim_base, dim_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
-    // initial counts -> prefixes, tile maps, tile numbering
-    BCK(cvg_launch_set_nh_batch(realloc_batch(b), b->d_tile_base, st));
     // kernels
     cudaLibrary_t lib = nullptr;
     BCKS(cvg_internal_load_module(ctx, batch_source(*b, dims), &lib));
@@ -456,7 +480,9 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
     int occ = 0;
     BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)b->fill, b->block, b->fill_smem));
     if (occ < 1) return cvg_internal_fail(CVG_ERR_INVALID, "batched fill kernel cannot be resident");
-    b->grid = occ * ctx->n_sm;
+    b->grid = std::min(occ * ctx->n_sm, b->max_ranges);
+    // initial counts -> prefixes, tile maps, tile numbering and the fill's ranges
+    BCK(cvg_launch_set_nh_batch(realloc_batch(b), batch_sched(b), st));
     BCK(cudaEventCreate(&b->ev0));
     BCK(cudaEventCreate(&b->ev1));
     BCK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));

@@ -79,7 +79,11 @@ struct cvg_batch_args {
     const cvg_fill_args *inst;    // [n_inst]
     const int *dims;              // [n_inst]
     const cvg_u64 *tile_base;     // [n_inst + 1] first global tile of each instance
+    const cvg_u64 *range_start;   // [n_ranges + 1] first global tile of each CTA's range
+    const cvg_u32 *range_inst;    // [n_ranges] an instance at or before range_start's tile
+    cvg_u64 *claim;               // [n_ranges] tiles claimed from each range (zero at launch)
     int n_inst;
+    int n_ranges;                 // = gridDim.x of the fill
     cvg_philox_keys keys;         // key schedule of the common seed
 };
 

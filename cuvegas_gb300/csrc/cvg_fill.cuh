@@ -949,40 +949,95 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 // ---------------------------------------------------------------------------
 // Batched fill: many independent integrals (different dimensions and sample
 // counts) in one persistent launch.  Tiles of all instances are numbered
-// globally (tile_base[i] = first tile of instance i this iteration); CTA b
-// takes a contiguous range of tiles, so it meets few instance changes.  On a
-// change it flushes the previous instance's histograms and loads the next
-// instance's grid.  DISP::run(dim, op) calls op(cvg_int<D>, cvg_int<P>) for
-// the dimensions present; DISP::fn<D> is the integrand of dimension D.
+// globally (tile_base[i] = first tile of instance i this iteration) and cut
+// into one contiguous range per CTA, of equal estimated cost (the tile-base
+// kernel weighs a tile by its instance's dimension).  A CTA claims tiles of
+// its own range first, then of the others' (cvg_batch_claim), so CTAs that
+// drew cheaper work take over the tail of heavier ranges.  While its claims
+// stay in one instance the CTA keeps that instance's grid and histograms in
+// shared memory; on a change it flushes the histograms and loads the next
+// grid.  DISP::run(dim, op) calls op(cvg_int<D>, cvg_int<P>) for the
+// dimensions present; DISP::fn<D> is the integrand of dimension D.
 // ---------------------------------------------------------------------------
 template <int V> struct cvg_int { static constexpr int value = V; };
 template <bool V> struct cvg_bool { static constexpr bool value = V; };
 
+// Block-wide claim of the next tiles.  Warp 0 looks at 32 ranges at a time,
+// starting at the CTA's own (ranges blockIdx.x, blockIdx.x + 1, ... modulo
+// n_ranges) and takes a quarter of what is left of the first range with
+// tiles unclaimed (at least one tile): the owner starts with long runs, the
+// last claims of a range are single tiles.  The claim is left in shared
+// memory, sh = {first tile t, end te, an instance at or before t, ranges
+// found used up}; it stays there until the next claim.  Returns t < te
+// (false once every range is used up).  Call from all threads of the block.
+__device__ __noinline__ bool cvg_batch_claim(const cvg_batch_args &b, cvg_u64 *sh)
+{
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int R = b.n_ranges;
+        int vv = (int)sh[3];
+        cvg_u64 got = 0, end = 0, gi = 0;
+        while (vv < R) {
+            const int o = vv + lane;
+            int v = 0;
+            cvg_u64 r0 = 0, len = 0, seen = 0;
+            bool avail = false;
+            if (o < R) {
+                v = (int)blockIdx.x + o;
+                if (v >= R) v -= R;
+                r0 = b.range_start[v];
+                len = b.range_start[v + 1] - r0;
+                seen = *(volatile const cvg_u64 *)&b.claim[v];
+                avail = seen < len;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, avail);
+            if (!m) { vv += 32; continue; }
+            const int src = __ffs(m) - 1;
+            cvg_u64 c0 = 0, k = 0;
+            if (lane == src) {
+                k = (len - seen) >> 2;
+                if (k == 0) k = 1;
+                c0 = atomicAdd(&b.claim[v], k);
+                if (c0 < len) {
+                    got = r0 + c0;
+                    end = r0 + (c0 + k < len ? c0 + k : len);
+                    gi = b.range_inst[v];
+                }
+            }
+            if (__shfl_sync(0xffffffffu, (int)(c0 < len), src)) {
+                got = __shfl_sync(0xffffffffu, got, src);
+                end = __shfl_sync(0xffffffffu, end, src);
+                gi = __shfl_sync(0xffffffffu, gi, src);
+                vv += src;                         // this range may hold more
+                break;
+            }
+            vv += src + 1;                         // raced to its end: next range
+        }
+        __syncwarp();
+        if (lane == 0) { sh[0] = got; sh[1] = end; sh[2] = gi; sh[3] = (cvg_u64)vv; }
+    }
+    __syncthreads();
+    return sh[0] < sh[1];
+}
 
 template <typename T, int BS, class DISP, int NI = 0>
 CVG_D void cvg_fill_batch(const cvg_batch_args &b)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
-    const cvg_u64 total = b.tile_base[b.n_inst];
-    const cvg_u64 chunk = (total + gridDim.x - 1) / gridDim.x;
-    cvg_u64 t = (cvg_u64)blockIdx.x * chunk;
-    const cvg_u64 t1 = min(t + chunk, total);
-    if (t >= t1) return;
-    int lo = 0, hi = b.n_inst - 1;            // instance holding tile t
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (b.tile_base[mid] <= t) lo = mid; else hi = mid - 1;
-    }
-    int i = lo;
-    while (t < t1) {
-        while (b.tile_base[i + 1] <= t) ++i;   // skip instances without tiles
-        const cvg_u64 tb = b.tile_base[i];
-        const cvg_u64 te = min(t1, b.tile_base[i + 1]);
+    __shared__ cvg_u64 sh[4];
+    if (threadIdx.x == 0) sh[3] = 0;
+    __syncwarp();
+    bool more = cvg_batch_claim(b, sh);
+    cvg_u64 t = sh[0];
+    int i = (int)sh[2];
+    while (more) {
+        while (b.tile_base[i + 1] <= t) ++i;   // instance holding tile t
+        const cvg_u64 t_in = t;
         const cvg_fill_args a = b.inst[i];
         DISP::run(b.dims[i], [&](auto Dc, auto Pc) {
             constexpr int D = decltype(Dc)::value, P = decltype(Pc)::value;
             using F = typename DISP::template fn<D>;
-            auto range = [&](auto Fx) {
+            auto session = [&](auto Fx) {
                 constexpr bool FIX = decltype(Fx)::value;
                 cvg_fill_smem<D, T, true, true, P, false> sm;
                 sm.carve(cvg_smem, a.n_intervals, a.tile_samples);
@@ -990,18 +1045,39 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
                 cvg_fill_setup<D, T, BS, true, true, P, false, FIX>(a, sm, cx);
                 __syncthreads();
                 const cvg_u64 S = a.nh_sum[a.n_cubes];
-                const cvg_u64 nt = b.tile_base[i + 1] - tb;
-                cvg_u32 nrare = 0;
-                cvg_u64 since = 0;
-                for (cvg_u64 lt = t - tb; lt < te - tb; ++lt) {
-                    if (since + (cvg_u64)a.tile_samples > CVG_HIST_MAX_RUN) {
-                        cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm, true);
-                        since = 0;
+                const cvg_u32 nt = (cvg_u32)(b.tile_base[i + 1] - b.tile_base[i]);
+                // tiles of this instance counted from its first (< 2^32)
+                cvg_u32 lt = (cvg_u32)(t - b.tile_base[i]);
+                cvg_u32 nrare = 0, since = 0;
+                while (true) {
+                    const cvg_u64 tb = b.tile_base[i], te = sh[1];
+                    const bool cont = te > tb + nt;    // the claim goes on in the next instance
+                    const cvg_u32 lstop = cont ? nt : (cvg_u32)(te - tb);
+                    bool ok = true;
+                    for (; lt < lstop; ++lt) {
+                        if (since + (cvg_u32)a.tile_samples > CVG_HIST_MAX_RUN) {
+                            cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm, true);
+                            since = 0;
+                        }
+                        since += (cvg_u32)a.tile_samples;
+                        if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX>(
+                                a, sm, cx, lt, nt, S, nullptr, nrare, b.keys)) {
+                            ok = false;   // inconsistent tile map (status set): this CTA stops
+                            break;
+                        }
                     }
-                    since += (cvg_u64)a.tile_samples;
-                    if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX>(
-                            a, sm, cx, lt, nt, S, nullptr, nrare, b.keys))
+                    if (!ok) { more = false; break; }
+                    if (cont) { t = b.tile_base[i] + nt; break; }
+                    more = cvg_batch_claim(b, sh);
+                    if (!more) break;
+                    t = sh[0];
+                    const cvg_u64 tb2 = b.tile_base[i];
+                    if (t < tb2 || t >= tb2 + nt) {    // another instance: flush, reload
+                        const int hint = (int)sh[2];
+                        if (t < tb2 || hint > i) i = hint;
                         break;
+                    }
+                    lt = (cvg_u32)(t - tb2);
                 }
                 cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm);
                 if (FIX) cvg_fill_count_rare(a, nrare);
@@ -1009,9 +1085,17 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
             // one histogram form per dimension here: a second copy of every
             // dimension's loop made the batched kernel spill (it is held to 64
             // registers per thread)
-            range(cvg_bool<cvg_hist_fixed<D, T>()>{});
+            session(cvg_bool<cvg_hist_fixed<D, T>()>{});
         });
-        t = te;
+        if (more && t == t_in) {                 // no variant for this dimension
+            const cvg_u64 te = sh[1], tn = b.tile_base[i + 1];
+            t = te < tn ? te : tn;
+            if (t >= te) {
+                more = cvg_batch_claim(b, sh);
+                t = sh[0];
+                i = (int)sh[2];
+            }
+        }
     }
 }
 

@@ -953,34 +953,78 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine_b(cvg
     }
 }
 
-// Global tile numbering of the next batched fill: tile_base[i] = first tile
-// of instance i, tile_base[n] = total (tiles per instance clamped to the
-// capacity of its tile map).
-__global__ void k_tile_base(cvg_realloc_batch B, cvg_u64 *tile_base)
+// Estimated cost of one tile of a dimension-D instance in the batched fill:
+// a sample's fixed work (tile set-up, cube runs, sums, loop) is about five
+// times the work it does per dimension (sampler, map, integrand factor, bin
+// sums).  The fill's claims correct what this estimate misses.
+__device__ __forceinline__ cvg_u64 cvg_batch_tile_cost(int dim) { return (cvg_u64)dim + 5u; }
+
+// Work split of the next batched fill.  tile_base[i] = first global tile of
+// instance i, tile_base[n] = total (tiles per instance clamped to the
+// capacity of its tile map); cost_base the same prefix over tile costs.  The
+// cost-weighted tile sequence is cut into n_ranges equal parts: range r
+// starts at the first tile whose cost prefix is >= C*r/n_ranges, so the
+// ranges are contiguous, ordered and cover every tile once.  One CTA of the
+// fill owns each range; the claim counters start at zero.
+__global__ void __launch_bounds__(1024) k_tile_base(cvg_realloc_batch B, cvg_batch_sched S)
 {
-    __shared__ cvg_u64 cnt[1024];
-    cvg_u64 carry = 0;
+    __shared__ cvg_u64 wt[32], wc[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    cvg_u64 carry_t = 0, carry_c = 0;
     for (int b0 = 0; b0 < B.n; b0 += blockDim.x) {
         const int i = b0 + threadIdx.x;
-        cvg_u64 c = 0;
+        cvg_u64 nt = 0, nc = 0;
         if (i < B.n) {
             const cvg_realloc_args &a = B.A[i];
-            const cvg_u64 S = a.nh_sum[a.n_cubes], TS = (cvg_u64)a.tile_samples;
-            c = (S + TS - 1) / TS;
-            if (c > a.max_tiles) c = a.max_tiles;
+            const cvg_u64 Sm = a.nh_sum[a.n_cubes], TS = (cvg_u64)a.tile_samples;
+            nt = (Sm + TS - 1) / TS;
+            if (nt > a.max_tiles) nt = a.max_tiles;
+            nc = nt * cvg_batch_tile_cost(a.dim);
         }
-        cnt[threadIdx.x] = c;
+        // block-wide inclusive scan of (nt, nc)
+        cvg_u64 st = nt, sc = nc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const cvg_u64 ut = __shfl_up_sync(0xffffffffu, st, o), uc = __shfl_up_sync(0xffffffffu, sc, o);
+            if (lane >= o) { st += ut; sc += uc; }
+        }
+        if (lane == 31) { wt[w] = st; wc[w] = sc; }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < (int)blockDim.x && b0 + k < B.n; ++k) {
-                const cvg_u64 v = cnt[k];
-                tile_base[b0 + k] = carry;
-                carry += v;
+        if (w == 0) {
+            cvg_u64 xt = lane < nw ? wt[lane] : 0, xc = lane < nw ? wc[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const cvg_u64 ut = __shfl_up_sync(0xffffffffu, xt, o), uc = __shfl_up_sync(0xffffffffu, xc, o);
+                if (lane >= o) { xt += ut; xc += uc; }
             }
+            if (lane < nw) { wt[lane] = xt; wc[lane] = xc; }
         }
         __syncthreads();
+        const cvg_u64 pt = carry_t + (w ? wt[w - 1] : 0) + st - nt;
+        const cvg_u64 pc = carry_c + (w ? wc[w - 1] : 0) + sc - nc;
+        if (i < B.n) { S.tile_base[i] = pt; S.cost_base[i] = pc; }
+        carry_t += wt[nw - 1];
+        carry_c += wc[nw - 1];
+        __syncthreads();   // wt / wc are rewritten by the next chunk
     }
-    if (threadIdx.x == 0) tile_base[B.n] = carry;
+    if (threadIdx.x == 0) { S.tile_base[B.n] = carry_t; S.cost_base[B.n] = carry_c; }
+    __syncthreads();
+    const cvg_u64 C = carry_c, R = (cvg_u64)S.n_ranges;
+    for (int r = threadIdx.x; r <= S.n_ranges; r += blockDim.x) {
+        if (r == S.n_ranges) { S.range_start[r] = carry_t; break; }
+        // c = floor(C * r / R) without overflow
+        const cvg_u64 c = (C / R) * (cvg_u64)r + (C % R) * (cvg_u64)r / R;
+        int lo = 0, hi = B.n - 1;                  // last instance with cost_base <= c
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.cost_base[mid] <= c) lo = mid; else hi = mid - 1;
+        }
+        const cvg_u64 wc1 = cvg_batch_tile_cost(B.A[lo].dim);
+        const cvg_u64 lt = (c - S.cost_base[lo] + wc1 - 1) / wc1;
+        S.range_start[r] = S.tile_base[lo] + lt;
+        S.range_inst[r] = (cvg_u32)lo;
+        S.claim[r] = 0;
+    }
 }
 
 __global__ void grid32(const double *x, float *x32, int n)
@@ -1272,7 +1316,7 @@ cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s
 }
 
 cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
-                                     cvg_u64 *tile_base, cudaStream_t s)
+                                     const cvg_batch_sched &S, cudaStream_t s)
 {
     (void)fast;
     k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);          // + finish per instance
@@ -1280,15 +1324,16 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
         k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);      // + scan per instance
         k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
     }
-    k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
+    k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
 }
 
-cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_base, cudaStream_t s)
+cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, const cvg_batch_sched &S,
+                                    cudaStream_t s)
 {
     k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
     k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
-    k_tile_base<<<1, 1024, 0, s>>>(B, tile_base);
+    k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
 }
 

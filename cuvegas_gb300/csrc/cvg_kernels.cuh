@@ -127,9 +127,19 @@ cudaError_t cvg_launch_pipe_bench(int kind, int blocks, int iters, double *sink,
 cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s);
 
 // Batched reallocation (+ the tile numbering of the next batched fill).
+// Work split of the next batched fill, written after each reallocation.
+struct cvg_batch_sched {
+    cvg_u64 *tile_base;           // [n+1] first global tile of each instance
+    cvg_u64 *cost_base;           // [n+1] cost-weighted prefix of the tiles
+    cvg_u64 *range_start;         // [n_ranges+1] first tile of each CTA's range
+    cvg_u32 *range_inst;          // [n_ranges] instance of range_start (or one before it)
+    cvg_u64 *claim;               // [n_ranges] claim counters, zeroed here
+    int n_ranges;
+};
 cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
-                                     cvg_u64 *tile_base, cudaStream_t s);
-cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, cvg_u64 *tile_base, cudaStream_t s);
+                                     const cvg_batch_sched &S, cudaStream_t s);
+cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, const cvg_batch_sched &S,
+                                    cudaStream_t s);
 cudaError_t cvg_launch_refine_batch(const cvg_refine_batch &B, int n_intervals, cudaStream_t s);
 
 // Set the calling thread's cvg_last_error() message (host code of the library).
