@@ -21,6 +21,9 @@ CANDIDATES = [(256, 16), (512, 8), (512, 12), (512, 16), (1024, 4), (1024, 8)]
 # single runs of large iterations run warp tiles (32 * spt samples per warp),
 # where larger tiles and 1024-thread blocks measured faster
 RUN_CANDIDATES = CANDIDATES + [(512, 24), (512, 32), (1024, 16), (1024, 24), (1024, 32)]
+# batched fills run warp tiles too; their largest dimension's variant holds
+# the kernel's registers, so 512- and 768-thread blocks stay in the set
+BATCH_CANDIDATES = [(512, 16), (512, 32), (768, 32), (1024, 16), (1024, 32)]
 _lock = threading.Lock()
 
 
@@ -97,12 +100,12 @@ def integrand_source(integrand):
 
 
 def tune_batch(ctx, source, instances, params_per_dim, precision, n_intervals=1024,
-               candidates=CANDIDATES):
+               candidates=BATCH_CANDIDATES):
     """Best (block, spt) for a batch: times one batched fill per candidate."""
     from .batch import Batch
     dims = sorted({int(i["dim"]) for i in instances})
     evals = sum(int(i.get("n_eval_it", 0)) for i in instances)
-    key = _key("batch%d" % len(instances), dims, precision, n_intervals, evals, source)
+    key = _key("batchwt%d" % len(instances), dims, precision, n_intervals, evals, source)
     hit = _load().get(key)
     if hit:
         return tuple(hit)

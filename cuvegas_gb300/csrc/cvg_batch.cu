@@ -199,6 +199,7 @@ cvg_batch_args batch_args(const cvg_batch_s *b)
     a.claim = b->d_claim;
     a.n_inst = b->n;
     a.n_ranges = b->grid;
+    a.max_claim = (cvg_u32)(CVG_HIST_MAX_RUN / (unsigned)b->TS);
     cvg_philox_schedule(b->p.seed, a.keys);
     return a;
 }
@@ -290,7 +291,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         delete b;
         return cvg_internal_fail(CVG_ERR_INVALID, "bad block / spt");
     }
-    b->TS = b->block * b->spt;
+    b->TS = 32 * b->spt;   // warp tiles
     b->max_ranges = 32 * std::max(1, ctx->n_sm);
     const int N = p.n_intervals;
     std::set<int> dims;
@@ -328,7 +329,7 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
     }
     tables_layout(b, nullptr, total);
     const int tsz = p.precision == CVG_PREC_FP32 ? 4 : 8;
-    b->fill_smem = cvg_fill_smem_bytes(dmax, N, tsz, 1, 1, 0, b->TS, pmax, b->block);
+    b->fill_smem = cvg_fill_smem_bytes(dmax, N, tsz, 1, 1, 0, b->TS, pmax, b->block, b->block / 32);
     // (+ the fill's few static bytes: its claim slots)
     if (b->fill_smem + 64 > (size_t)ctx->smem_optin) {
         delete b;

@@ -19,6 +19,9 @@ typedef long long cvg_i64;
 #define CVG_KSTAT_BAD_TILE 1u      // tile map inconsistent with nh_sum
 #define CVG_KSTAT_NONFINITE 2u     // a non-finite per-cube estimate was seen
 #define CVG_KSTAT_TIMEOUT 4u       // a bounded wait ran out (the results are not valid)
+// Samples a CTA adds to its shared-memory bin histograms between flushes
+// (bin counts stay below 2^24)
+#define CVG_HIST_MAX_RUN 0x00FFF000u
 
 // Philox4x32-10 key schedule of one seed: round r uses (k0 + r*0x9E3779B9,
 // k1 + r*0xBB67AE85).  Kept in the kernel arguments (constant bank), so the
@@ -84,6 +87,7 @@ struct cvg_batch_args {
     cvg_u64 *claim;               // [n_ranges] tiles claimed from each range (zero at launch)
     int n_inst;
     int n_ranges;                 // = gridDim.x of the fill
+    cvg_u32 max_claim;            // tiles one claim may take (its samples < CVG_HIST_MAX_RUN)
     cvg_philox_keys keys;         // key schedule of the common seed
 };
 

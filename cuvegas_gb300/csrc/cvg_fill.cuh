@@ -195,7 +195,6 @@ CVG_D int cvg_bin(double z, int N, double, double &frac)
 #define CVG_HIST_GROUP 8
 #endif
 #define CVG_HIST_CNT_MASK 0x00FFFFFFu
-#define CVG_HIST_MAX_RUN 0x00FFF000u   // samples between flushes (counts < 2^24)
 // Fixed-point bin sums are used by the FP32 form up to this dimension;
 // above it the shared-memory float atomics are kept.
 #ifndef CVG_HIST_FIX_MAX_DIM
@@ -951,13 +950,16 @@ CVG_D void cvg_fill_body(const cvg_fill_args &a)
 // counts) in one persistent launch.  Tiles of all instances are numbered
 // globally (tile_base[i] = first tile of instance i this iteration) and cut
 // into one contiguous range per CTA, of equal estimated cost (the tile-base
-// kernel weighs a tile by its instance's dimension).  A CTA claims tiles of
-// its own range first, then of the others' (cvg_batch_claim), so CTAs that
-// drew cheaper work take over the tail of heavier ranges.  While its claims
-// stay in one instance the CTA keeps that instance's grid and histograms in
-// shared memory; on a change it flushes the histograms and loads the next
-// grid.  DISP::run(dim, op) calls op(cvg_int<D>, cvg_int<P>) for the
-// dimensions present; DISP::fn<D> is the integrand of dimension D.
+// kernel weighs a tile by its instance's dimension).  A CTA claims chunks of
+// tiles from its own range first, then from the others' (cvg_batch_claim), so
+// CTAs that drew cheaper work take over the tail of heavier ranges.  Tiles
+// are warp tiles (32 * spt samples): within a chunk each warp takes the next
+// tile from a shared counter, with no block barrier until the chunk is used
+// up.  While its claims stay in one instance the CTA keeps that instance's
+// grid and histograms in shared memory; on a change it flushes the
+// histograms and loads the next grid.  DISP::run(dim, op) calls
+// op(cvg_int<D>, cvg_int<P>) for the dimensions present; DISP::fn<D> is the
+// integrand of dimension D.
 // ---------------------------------------------------------------------------
 template <int V> struct cvg_int { static constexpr int value = V; };
 template <bool V> struct cvg_bool { static constexpr bool value = V; };
@@ -965,8 +967,8 @@ template <bool V> struct cvg_bool { static constexpr bool value = V; };
 // Block-wide claim of the next tiles.  Warp 0 looks at 32 ranges at a time,
 // starting at the CTA's own (ranges blockIdx.x, blockIdx.x + 1, ... modulo
 // n_ranges) and takes a quarter of what is left of the first range with
-// tiles unclaimed (at least one tile): the owner starts with long runs, the
-// last claims of a range are single tiles.  The claim is left in shared
+// tiles unclaimed (at least one tile, at most max_claim): the owner starts
+// with long runs, the last claims of a range are single tiles.  The claim is left in shared
 // memory, sh = {first tile t, end te, an instance at or before t, ranges
 // found used up}; it stays there until the next claim.  Returns t < te
 // (false once every range is used up).  Call from all threads of the block.
@@ -996,6 +998,7 @@ __device__ __noinline__ bool cvg_batch_claim(const cvg_batch_args &b, cvg_u64 *s
             cvg_u64 c0 = 0, k = 0;
             if (lane == src) {
                 k = (len - seen) >> 2;
+                if (k > (cvg_u64)b.max_claim) k = b.max_claim;
                 if (k == 0) k = 1;
                 c0 = atomicAdd(&b.claim[v], k);
                 if (c0 < len) {
@@ -1025,11 +1028,13 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
 {
     extern __shared__ __align__(16) unsigned char cvg_smem[];
     __shared__ cvg_u64 sh[4];
-    if (threadIdx.x == 0) sh[3] = 0;
+    __shared__ cvg_u32 s_tile[2];   // next tile of the chunk (counted in its instance), bad-tile flag
+    if (threadIdx.x == 0) { sh[3] = 0; s_tile[1] = 0; }
     __syncwarp();
     bool more = cvg_batch_claim(b, sh);
     cvg_u64 t = sh[0];
     int i = (int)sh[2];
+    const cvg_u32 lane = threadIdx.x & 31;
     while (more) {
         while (b.tile_base[i + 1] <= t) ++i;   // instance holding tile t
         const cvg_u64 t_in = t;
@@ -1040,51 +1045,60 @@ CVG_D void cvg_fill_batch(const cvg_batch_args &b)
             auto session = [&](auto Fx) {
                 constexpr bool FIX = decltype(Fx)::value;
                 cvg_fill_smem<D, T, true, true, P, false> sm;
-                sm.carve(cvg_smem, a.n_intervals, a.tile_samples);
+                sm.carve(cvg_smem, a.n_intervals, a.tile_samples, BS / 32);
                 cvg_fill_ctx<T> cx;
                 cvg_fill_setup<D, T, BS, true, true, P, false, FIX>(a, sm, cx);
-                __syncthreads();
                 const cvg_u64 S = a.nh_sum[a.n_cubes];
                 const cvg_u32 nt = (cvg_u32)(b.tile_base[i + 1] - b.tile_base[i]);
                 // tiles of this instance counted from its first (< 2^32)
-                cvg_u32 lt = (cvg_u32)(t - b.tile_base[i]);
+                cvg_u32 l0 = (cvg_u32)(t - b.tile_base[i]);
                 cvg_u32 nrare = 0, since = 0;
+                if (threadIdx.x == 0) s_tile[0] = l0;
+                __syncthreads();
                 while (true) {
                     const cvg_u64 tb = b.tile_base[i], te = sh[1];
                     const bool cont = te > tb + nt;    // the claim goes on in the next instance
                     const cvg_u32 lstop = cont ? nt : (cvg_u32)(te - tb);
-                    bool ok = true;
-                    for (; lt < lstop; ++lt) {
-                        if (since + (cvg_u32)a.tile_samples > CVG_HIST_MAX_RUN) {
-                            cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm, true);
-                            since = 0;
-                        }
-                        since += (cvg_u32)a.tile_samples;
-                        if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX>(
+                    // warp tiles of the chunk, one at a time from the shared counter:
+                    // no barrier until the chunk is used up
+                    while (true) {
+                        cvg_u32 lt = 0;
+                        if (lane == 0) lt = atomicAdd(&s_tile[0], 1u);
+                        lt = __shfl_sync(0xffffffffu, lt, 0);
+                        if (lt >= lstop) break;
+                        if (!cvg_fill_tile<D, T, BS, true, true, false, P, false, F, NI, FIX, true>(
                                 a, sm, cx, lt, nt, S, nullptr, nrare, b.keys)) {
-                            ok = false;   // inconsistent tile map (status set): this CTA stops
+                            if (lane == 0) s_tile[1] = 1u;   // inconsistent tile map (status set)
                             break;
                         }
                     }
-                    if (!ok) { more = false; break; }
-                    if (cont) { t = b.tile_base[i] + nt; break; }
+                    since += (lstop - l0) * (cvg_u32)a.tile_samples;
+                    __syncthreads();                   // every warp is done with the chunk
+                    if (s_tile[1]) { more = false; break; }
+                    if (cont) { t = tb + nt; break; }
                     more = cvg_batch_claim(b, sh);
                     if (!more) break;
                     t = sh[0];
-                    const cvg_u64 tb2 = b.tile_base[i];
-                    if (t < tb2 || t >= tb2 + nt) {    // another instance: flush, reload
+                    if (t < tb || t >= tb + nt) {      // another instance: flush, reload
                         const int hint = (int)sh[2];
-                        if (t < tb2 || hint > i) i = hint;
+                        if (t < tb || hint > i) i = hint;
                         break;
                     }
-                    lt = (cvg_u32)(t - tb2);
+                    l0 = (cvg_u32)(t - tb);
+                    const cvg_u64 te2 = sh[1] < tb + nt ? sh[1] : tb + nt;
+                    // counts stay below 2^24 (a claim holds at most max_claim tiles)
+                    if (since + (cvg_u32)(te2 - t) * (cvg_u32)a.tile_samples > CVG_HIST_MAX_RUN) {
+                        cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm, true);
+                        since = 0;
+                    }
+                    if (threadIdx.x == 0) s_tile[0] = l0;
+                    __syncthreads();
                 }
                 cvg_fill_flush<D, T, BS, true, true, P, false, NI, FIX>(a, sm);
                 if (FIX) cvg_fill_count_rare(a, nrare);
             };
             // one histogram form per dimension here: a second copy of every
-            // dimension's loop made the batched kernel spill (it is held to 64
-            // registers per thread)
+            // dimension's loop made the batched kernel spill
             session(cvg_bool<cvg_hist_fixed<D, T>()>{});
         });
         if (more && t == t_in) {                 // no variant for this dimension

@@ -954,10 +954,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine_b(cvg
 }
 
 // Estimated cost of one tile of a dimension-D instance in the batched fill:
-// a sample's fixed work (tile set-up, cube runs, sums, loop) is about five
-// times the work it does per dimension (sampler, map, integrand factor, bin
-// sums).  The fill's claims correct what this estimate misses.
-__device__ __forceinline__ cvg_u64 cvg_batch_tile_cost(int dim) { return (cvg_u64)dim + 5u; }
+// its time per sample, measured on product-peak instances of d = 2..12, grows
+// by about 1/20 of the d = 2 time per added dimension.  The fill's claims
+// correct what this estimate misses.
+__device__ __forceinline__ cvg_u64 cvg_batch_tile_cost(int dim) { return (cvg_u64)dim + 20u; }
 
 // Work split of the next batched fill.  tile_base[i] = first global tile of
 // instance i, tile_base[n] = total (tiles per instance clamped to the

@@ -49,7 +49,7 @@ def test_batch_fp32_family_against_analytic(ctx):
     FP32 compensated, CUDA graph, autotuned tiles, 10 iterations."""
     insts = _instances(64, 2, lo=4, hi=6)
     block, spt = autotune.tune_batch(ctx, I.PRODPEAK, insts, PPD, L.PREC_FP32)
-    assert (block, spt) in autotune.CANDIDATES
+    assert (block, spt) in autotune.BATCH_CANDIDATES
     with B.Batch(ctx, I.PRODPEAK, insts, PPD, max_it=10, skip=5, seed=3,
                  precision=L.PREC_FP32, graph=True, block=block, spt=spt) as b:
         b.iterate(10)
