@@ -56,7 +56,8 @@ struct inst_host {
     double *scale_ss;
     int *bin_exp;
     cvg_u32 *done;
-    cvg_u64 *nh_sum, *bsums;
+    cvg_u64 *nh_sum, *bsums, *lb;
+    cvg_u32 *lb_ctl;
     cvg_acc_dev *acc;
 };
 
@@ -76,7 +77,7 @@ struct cvg_batch_s {
     cvg_realloc_args *d_realloc = nullptr;
     cvg_refine_args *d_refine = nullptr;
     int *d_dims = nullptr;
-    unsigned *d_blk_base = nullptr, *d_dim_base = nullptr;
+    unsigned *d_blk_base = nullptr, *d_dim_base = nullptr, *d_blk_inst = nullptr;
     cvg_u64 *d_tile_base = nullptr, *d_cost_base = nullptr;
     cvg_u64 *d_range_start = nullptr, *d_claim = nullptr;
     cvg_u32 *d_range_inst = nullptr;
@@ -117,6 +118,8 @@ void inst_layout(inst_host &h, int N, int max_it, char *base, size_t &off)
     place(h.tile_cube, sizeof(cvg_u32) * h.max_tiles, base, off);
     place(h.partials, sizeof(double) * 4 * h.nb, base, off);
     place(h.bsums, sizeof(cvg_u64) * (h.nb + 1), base, off);
+    place(h.lb, sizeof(cvg_u64) * h.nb, base, off);
+    place(h.lb_ctl, 16, base, off);
     place(h.stats, sizeof(double) * 3 * max_it, base, off);
     place(h.acc, sizeof(cvg_acc_dev), base, off);
     place(h.iteration, 16, base, off);
@@ -138,6 +141,7 @@ void tables_layout(cvg_batch_s *b, char *base, size_t &off)
     place(b->d_refine, sizeof(cvg_refine_args) * n, base, off);
     place(b->d_dims, sizeof(int) * n, base, off);
     place(b->d_blk_base, sizeof(unsigned) * (n + 1), base, off);
+    place(b->d_blk_inst, sizeof(unsigned) * b->total_blocks, base, off);
     place(b->d_dim_base, sizeof(unsigned) * (n + 1), base, off);
     place(b->d_tile_base, sizeof(cvg_u64) * (n + 1), base, off);
     place(b->d_cost_base, sizeof(cvg_u64) * (n + 1), base, off);
@@ -209,7 +213,9 @@ cvg_realloc_batch realloc_batch(const cvg_batch_s *b)
     cvg_realloc_batch B{};
     B.A = b->d_realloc;
     B.blk_base = b->d_blk_base;
+    B.blk_inst = b->d_blk_inst;
     B.total_blocks = b->total_blocks;
+    B.one_pass = 1;
     B.n = b->n;
     return B;
 }
@@ -321,6 +327,11 @@ cvg_status cvg_batch_create(cvg_context ctx, const char *source, int32_t abi, in
         h.v_cubes = std::pow(1.0 / h.n_strat, (double)h.dim);
         h.nh0 = (cvg_u32)std::max<int64_t>(2, (int64_t)(1.0 / (double)h.n_cubes * (double)h.n_eval_it));
         h.nb = cvg_realloc_blocks(h.n_cubes);
+        if ((uint64_t)b->total_blocks + h.nb > 0x7FFFFFFFull) {
+            delete b;
+            return cvg_internal_fail(CVG_ERR_INVALID, "batch: too many hypercubes in all");
+        }
+        b->total_blocks += h.nb;
         h.max_tiles = (s_max + b->TS - 1) / b->TS + 1;
         dims.insert(h.dim);
         dmax = std::max(dmax, h.dim);
@@ -449,6 +460,8 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         r.hist_state = nullptr;
         r.dim = D;
         r.adapt = (p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
+        r.lb = h.lb;            // one-pass allocation; the words start at zero (arena)
+        r.lb_ctl = h.lb_ctl;
         cvg_refine_args &q = hq[i];
         q.x_edges = h.x_edges;
         q.x_edges32 = h.x_edges32;
@@ -463,13 +476,18 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         blk_base[i + 1] = blk_base[i] + h.nb;
         dim_base[i + 1] = dim_base[i] + D;
     }
-    b->total_blocks = blk_base[n];
+    if (b->total_blocks != blk_base[n]) return cvg_internal_fail(CVG_ERR_STATE, "batch block count mismatch");
+    std::vector<unsigned> blk_inst(b->total_blocks);
+    for (int i = 0; i < n; ++i)
+        for (unsigned k = blk_base[i]; k < blk_base[i + 1]; ++k) blk_inst[k] = (unsigned)i;
     b->total_dims = dim_base[n];
     BCK(cudaMemcpyAsync(b->d_fill, hf.data(), sizeof(cvg_fill_args) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_realloc, hr.data(), sizeof(cvg_realloc_args) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_refine, hq.data(), sizeof(cvg_refine_args) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_dims, hdims.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_blk_base, blk_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
+    BCK(cudaMemcpyAsync(b->d_blk_inst, blk_inst.data(), sizeof(unsigned) * b->total_blocks,
+                        cudaMemcpyHostToDevice, st));
     BCK(cudaMemcpyAsync(b->d_dim_base, dim_base.data(), sizeof(unsigned) * (n + 1), cudaMemcpyHostToDevice, st));
     // kernels
     cudaLibrary_t lib = nullptr;
@@ -579,6 +597,8 @@ cvg_status cvg_batch_results(cvg_batch b, cvg_result *out, double *it_res, doubl
     }
     BCK(cudaMemcpyAsync(&status, b->d_status, sizeof(status), cudaMemcpyDeviceToHost, st));
     BCK(cudaStreamSynchronize(st));
+    if (status & CVG_KSTAT_TIMEOUT)
+        return cvg_internal_fail(CVG_ERR_KERNEL, "batched reallocation: a look-back wait ran out");
     if (status & CVG_KSTAT_BAD_TILE)
         return cvg_internal_fail(CVG_ERR_KERNEL, "batched fill found an inconsistent tile map");
     const int done = std::min(b->it_done, M);

@@ -526,10 +526,8 @@ __device__ __forceinline__ cvg_u64 lb_word(cvg_u32 epoch, cvg_u64 flag, cvg_u64 
 // Epochs run 1 .. 2^30 - 1 (0 marks a word never written).
 __device__ __forceinline__ cvg_u32 lb_next_epoch(cvg_u32 e) { return e % 0x3FFFFFFFu + 1u; }
 
-// 8 CTAs per SM (32 registers; a few bytes spill): more blocks in their
-// look-back at once (C2: 76.9 -> 69.6 us against 6 CTAs at 40 registers)
 template <int MODE>
-__global__ void __launch_bounds__(RB, 8) k3_alloc(cvg_realloc_args a, unsigned nb)
+__device__ __forceinline__ void k3_alloc_dev(const cvg_realloc_args &a, unsigned nb)
 {
     __shared__ cvg_u64 scratch[33];
     __shared__ unsigned s_blk;
@@ -664,6 +662,14 @@ __global__ void __launch_bounds__(RB, 8) k3_alloc(cvg_realloc_args a, unsigned n
         a.lb_ctl[0] = 0u;
         a.lb_ctl[1] = epoch;
     }
+}
+
+// 8 CTAs per SM (32 registers; a few bytes spill): more blocks in their
+// look-back at once (C2: 76.9 -> 69.6 us against 6 CTAs at 40 registers)
+template <int MODE>
+__global__ void __launch_bounds__(RB, 8) k3_alloc(cvg_realloc_args a, unsigned nb)
+{
+    k3_alloc_dev<MODE>(a, nb);
 }
 
 
@@ -910,7 +916,7 @@ __device__ __forceinline__ int find_inst(const unsigned *base, int n, unsigned b
 
 __global__ void __launch_bounds__(RB) k3_results_b(cvg_realloc_batch B)
 {
-    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const int i = (int)B.blk_inst[blockIdx.x];
     const cvg_realloc_args a = B.A[i];
     if (a.fast_pow) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
     else k3_results_dev(a, blockIdx.x - B.blk_base[i]);
@@ -922,7 +928,7 @@ __global__ void __launch_bounds__(RB) k3_results_b(cvg_realloc_batch B)
 
 __global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
 {
-    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const int i = (int)B.blk_inst[blockIdx.x];
     const cvg_realloc_args a = B.A[i];
     if (!a.adapt && mode != 1) return;
     k3_count_dev(a, mode == 0 ? (a.fast_pow ? 2 : 0) : mode, blockIdx.x - B.blk_base[i]);
@@ -934,10 +940,22 @@ __global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
 
 __global__ void __launch_bounds__(RB) k3_apply_b(cvg_realloc_batch B, int mode)
 {
-    const int i = find_inst(B.blk_base, B.n, blockIdx.x);
+    const int i = (int)B.blk_inst[blockIdx.x];
     const cvg_realloc_args a = B.A[i];
     if (!a.adapt && mode != 1) return;
     k3_apply_dev(a, cvg_realloc_blocks(a.n_cubes), blockIdx.x - B.blk_base[i]);
+}
+
+// One-pass allocation of every instance (instances with look-back words):
+// a block's chunk within its instance comes from the instance's ticket, so
+// the blocks an instance's look-back waits on have started before it.
+template <int MODE>
+__global__ void __launch_bounds__(RB, 8) k3_alloc_b(cvg_realloc_batch B)
+{
+    const int i = (int)B.blk_inst[blockIdx.x];
+    const cvg_realloc_args &a = B.A[i];
+    if (!a.adapt && MODE != 1) return;
+    k3_alloc_dev<MODE>(a, B.blk_base[i + 1] - B.blk_base[i]);
 }
 
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine_b(cvg_refine_batch B)
@@ -1318,11 +1336,15 @@ cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s
 cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
                                      const cvg_batch_sched &S, cudaStream_t s)
 {
-    (void)fast;
     k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);          // + finish per instance
     if (adapt) {
-        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);      // + scan per instance
-        k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
+        if (B.one_pass) {
+            if (fast) k3_alloc_b<2><<<B.total_blocks, RB, 0, s>>>(B);
+            else k3_alloc_b<0><<<B.total_blocks, RB, 0, s>>>(B);
+        } else {
+            k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);  // + scan per instance
+            k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
+        }
     }
     k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
@@ -1331,8 +1353,12 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
 cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, const cvg_batch_sched &S,
                                     cudaStream_t s)
 {
-    k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
-    k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
+    if (B.one_pass) {
+        k3_alloc_b<1><<<B.total_blocks, RB, 0, s>>>(B);
+    } else {
+        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
+        k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
+    }
     k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
 }

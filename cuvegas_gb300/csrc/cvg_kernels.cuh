@@ -84,8 +84,10 @@ enum { CVG_REALLOC_CHUNK = 2048, CVG_REFINE_BLOCK = 1024, CVG_REFINE_MAX_N = 409
 struct cvg_realloc_batch {
     const cvg_realloc_args *A;    // [n]
     const unsigned *blk_base;     // [n+1] prefix of reallocation blocks
+    const unsigned *blk_inst;     // [total_blocks] instance of each block
     unsigned total_blocks;
     int n;
+    int one_pass;                 // 1: every instance has look-back words (k3_alloc)
 };
 struct cvg_refine_batch {
     const cvg_refine_args *R;     // [n]
