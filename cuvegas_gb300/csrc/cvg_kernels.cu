@@ -762,15 +762,20 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
     bool ok = a.adapt && dsum > 0.0 && isfinite(dsum);
 
     if (ok) {
-        // smoothWeights (src/main.cu:120-145)
+        // smoothWeights (src/main.cu:120-145).  The FP32 form (ex) multiplies
+        // by 1/(8 d_sum) instead of dividing per bin (FP64 divisions are the
+        // costly part of this kernel; a one-rounding difference in the
+        // smoothed weight is far inside that form's tolerance); the FP64 form
+        // keeps the reference's division.
+        const double r8 = ex ? 1.0 / (8.0 * dsum) : 0.0;
         double p2 = 0.0;
         for (int i = i0 + tid; i < i1; i += KB) {
             const double wm = i > 0 ? w[i - i0] : 0.0, wc = w[i - i0 + 1];
             const double wp = i < N - 1 ? w[i - i0 + 2] : 0.0;
             double t;
-            if (i == 0) t = (7.0 * wc + wp) / (8.0 * dsum);
-            else if (i == N - 1) t = (wm + 7.0 * wc) / (8.0 * dsum);
-            else t = (wm + 6.0 * wc + wp) / (8.0 * dsum);
+            const double num = i == 0 ? 7.0 * wc + wp
+                             : (i == N - 1 ? wm + 7.0 * wc : wm + 6.0 * wc + wp);
+            t = ex ? num * r8 : num / (8.0 * dsum);
             if (t != 0) {
                 // ((t-1)/ln t)^alpha; alpha = 0.5 (the default) as a square
                 // root, correctly rounded and several times cheaper than pow
@@ -842,14 +847,22 @@ __device__ __forceinline__ void k4_refine_dev(const cvg_refine_args &a, const in
                 }
                 const int o = lo;
                 const double acc = (k + 1) * delta - (o > 0 ? fcs[o - 1] : 0.0);
-                const double xn = fma(acc / fsw[o], xo[o + 1] - xo[o], xo[o]);
-                xe[k + 1] = xn;
-                xe32[k + 1] = (float)xn;
-                // new bin k ends in old bin o, where it is delta/fsw[o] of o's
-                // width wide: its samples' (f*jac)^2 scale by that ratio squared
                 if (ex) {
-                    const double rr = fsw[o] > 0.0 ? delta / fsw[o] : 1.0;
+                    // FP32 form: one reciprocal of the old bin's weight for
+                    // the edge and the exponent
+                    const double rw = 1.0 / fsw[o];
+                    const double xn = fma(acc * rw, xo[o + 1] - xo[o], xo[o]);
+                    xe[k + 1] = xn;
+                    xe32[k + 1] = (float)xn;
+                    // new bin k ends in old bin o, where it is delta/fsw[o] of
+                    // o's width wide: its samples' (f*jac)^2 scale by that
+                    // ratio squared
+                    const double rr = fsw[o] > 0.0 ? delta * rw : 1.0;
                     eb[k - i0] = k4_exponent(fw[o] * rr * rr);
+                } else {
+                    const double xn = fma(acc / fsw[o], xo[o + 1] - xo[o], xo[o]);
+                    xe[k + 1] = xn;
+                    xe32[k + 1] = (float)xn;
                 }
             }
             if (ex && i1 == N && i0 < N && tid == 0) {
@@ -914,11 +927,13 @@ __device__ __forceinline__ int find_inst(const unsigned *base, int n, unsigned b
     return lo;
 }
 
-__global__ void __launch_bounds__(RB) k3_results_b(cvg_realloc_batch B)
+// one form per launch (the batch's precision), 4 blocks per SM as k3_results_f32
+template <bool FAST>
+__global__ void __launch_bounds__(RB, 4) k3_results_b(cvg_realloc_batch B)
 {
     const int i = (int)B.blk_inst[blockIdx.x];
-    const cvg_realloc_args a = B.A[i];
-    if (a.fast_pow) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
+    const cvg_realloc_args &a = B.A[i];
+    if (FAST) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
     else k3_results_dev(a, blockIdx.x - B.blk_base[i]);
     const unsigned nb = B.blk_base[i + 1] - B.blk_base[i];
     if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
@@ -1336,7 +1351,8 @@ cudaError_t cvg_launch_fill_u32(cvg_u32 *p, cvg_u32 v, cvg_u64 n, cudaStream_t s
 cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool fast,
                                      const cvg_batch_sched &S, cudaStream_t s)
 {
-    k3_results_b<<<B.total_blocks, RB, 0, s>>>(B);          // + finish per instance
+    if (fast) k3_results_b<true><<<B.total_blocks, RB, 0, s>>>(B);    // + finish per instance
+    else k3_results_b<false><<<B.total_blocks, RB, 0, s>>>(B);
     if (adapt) {
         if (B.one_pass) {
             if (fast) k3_alloc_b<2><<<B.total_blocks, RB, 0, s>>>(B);
