@@ -227,6 +227,39 @@ def fill_roofline(ctx, evals_per_launch, mean_ms, sm_mhz):
     return out
 
 
+def c5_roofline(ctx, evals_per_launch, mean_ms, sm_mhz):
+    """C5's fill (corner peak, d=16) against the ceilings the workload names:
+    FP32 pipe (FP32 instructions per evaluation, ncu, x evaluations/s against
+    the live FP32 FMA peak / 2), SFU (ncu's XU-pipe share of the same
+    launch), HBM (DRAM bytes per evaluation of the full 1e9 workload, ncu, x
+    evaluations/s against the measured copy bandwidth) and instruction issue
+    (instructions per evaluation x evaluations/s against 152 SMs x 4 warp
+    instructions per clock), which binds."""
+    rate = evals_per_launch / (mean_ms * 1e-3)
+    clk = (sm_mhz or 2070.0) * 1e6
+    issue = N_SM * 4 * 32 * clk / 1e12
+    src = "fill_corner_d16_counts.txt"
+    ipe = profile_value(src, "inst_per_eval")
+    fpe = profile_value(src, "fp32_inst_per_eval")
+    bpe = profile_value(src, "dram_bytes_per_eval")
+    out = {"bound": "issue", "evals_per_s_fill": rate, "fill_ms_mean": mean_ms,
+           "evals_per_launch": evals_per_launch, "issue_clock_mhz": clk / 1e6,
+           "counts_source": "profiles/" + src}
+    if ipe:
+        out.update({"instructions_per_eval": ipe, "achieved": rate * ipe / 1e12, "peak": issue,
+                    "unit": "T thread instructions/s", "frac": rate * ipe / 1e12 / issue})
+    if fpe:
+        p_fp32 = live_peak(ctx, 0) / 2.0
+        out.update({"fp32_inst_per_eval": fpe, "fp32_achieved": rate * fpe / 1e12,
+                    "fp32_peak": p_fp32, "fp32_unit": "T FP32 instructions/s",
+                    "fp32_pipe_frac": rate * fpe / 1e12 / p_fp32})
+    out["sfu_pipe_pct_ncu"] = profile_value(src, "ncu_xu_pipe_pct")
+    if bpe:
+        out.update({"dram_bytes_per_eval": bpe, "hbm_gbs": rate * bpe / 1e9,
+                    "hbm_peak_gbs": HBM_GBS, "hbm_frac": rate * bpe / 1e9 / HBM_GBS})
+    return out
+
+
 def plain_roofline(ctx, evals_per_launch, mean_ms):
     """FP64-pipe roofline of the plain (FP64) fill.  The FP64 pipe executes
     one FMA, add or multiply per lane per issue, so its ceiling is the live
@@ -465,6 +498,10 @@ def summary_c5(ctx, stream, torch, quick=False, evals=None):
            "iterations": 20}
     m = run_timed(f, 16, n_it, 20, L.PREC_FP32, stream, torch, th, nh_stats=True)
     out["chosen"] = _form_summary(m, 20, exact, L.PREC_FP32)
+    if m["fills"]:
+        fills = m["fills"][1:] if len(m["fills"]) > 2 else m["fills"]
+        out["chosen"]["roofline"] = c5_roofline(ctx, n_it, sum(fills) / len(fills),
+                                                m["clk"].get("sm_mhz"))
     if not quick:
         # plain: graph-replayed iterations only (no separate fill-timed run)
         m = run_timed(f, 16, n_it, 20, L.PREC_FP64, stream, torch, th, fill_times=False)
