@@ -101,23 +101,27 @@ def integrand_source(integrand):
 
 def tune_batch(ctx, source, instances, params_per_dim, precision, n_intervals=1024,
                candidates=BATCH_CANDIDATES):
-    """Best (block, spt) for a batch: times one batched fill per candidate."""
+    """Best (block, spt) for a batch: per candidate, the batched fills of
+    iterations 1-3 (after the first adaptation; the fill times differ most
+    between candidates in these early iterations)."""
     from .batch import Batch
     dims = sorted({int(i["dim"]) for i in instances})
     evals = sum(int(i.get("n_eval_it", 0)) for i in instances)
-    key = _key("batchwt%d" % len(instances), dims, precision, n_intervals, evals, source)
+    key = _key("batchwt3_%d" % len(instances), dims, precision, n_intervals, evals, source)
     hit = _load().get(key)
     if hit:
         return tuple(hit)
     best, best_ms = None, float("inf")
     for block, spt in candidates:
         try:
-            with Batch(ctx, source, instances, params_per_dim, max_it=3, skip=0,
+            with Batch(ctx, source, instances, params_per_dim, max_it=4, skip=0,
                        n_intervals=n_intervals, precision=precision, graph=False, block=block,
                        spt=spt) as b:
-                b.iterate(2)            # warm, adapted once
-                b.iterate(1)            # timed (last eager fill)
-                ms = _batch_fill_ms(b)
+                b.iterate(1)            # iteration 0: uniform grid, not timed
+                ms = 0.0
+                for _ in range(3):      # each eager iteration times its own fill
+                    b.iterate(1)
+                    ms += _batch_fill_ms(b)
         except L.CuvegasError:
             continue
         if ms < best_ms:
