@@ -215,7 +215,6 @@ cvg_realloc_batch realloc_batch(const cvg_batch_s *b)
     B.blk_base = b->d_blk_base;
     B.blk_inst = b->d_blk_inst;
     B.total_blocks = b->total_blocks;
-    B.one_pass = 1;
     B.n = b->n;
     return B;
 }

@@ -914,8 +914,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(KB) k4_refine(cvg_r
 
 // ---------------------------------------------------------------------------
 // Batched forms: one launch covers the blocks (or clusters) of every
-// instance; a block finds its instance by binary search over the prefix of
-// blocks per instance.
+// instance.  A reallocation block finds its instance in a block-to-instance
+// table; a refinement cluster by binary search over the prefix of
+// dimensions per instance.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int find_inst(const unsigned *base, int n, unsigned b)
 {
@@ -941,29 +942,9 @@ __global__ void __launch_bounds__(RB, 4) k3_results_b(cvg_realloc_batch B)
 
 
 
-__global__ void __launch_bounds__(RB) k3_count_b(cvg_realloc_batch B, int mode)
-{
-    const int i = (int)B.blk_inst[blockIdx.x];
-    const cvg_realloc_args a = B.A[i];
-    if (!a.adapt && mode != 1) return;
-    k3_count_dev(a, mode == 0 ? (a.fast_pow ? 2 : 0) : mode, blockIdx.x - B.blk_base[i]);
-    const unsigned nb = B.blk_base[i + 1] - B.blk_base[i];
-    if (last_block(&a.done[1], nb)) k3_scan_dev(a, nb);
-}
-
-
-
-__global__ void __launch_bounds__(RB) k3_apply_b(cvg_realloc_batch B, int mode)
-{
-    const int i = (int)B.blk_inst[blockIdx.x];
-    const cvg_realloc_args a = B.A[i];
-    if (!a.adapt && mode != 1) return;
-    k3_apply_dev(a, cvg_realloc_blocks(a.n_cubes), blockIdx.x - B.blk_base[i]);
-}
-
-// One-pass allocation of every instance (instances with look-back words):
-// a block's chunk within its instance comes from the instance's ticket, so
-// the blocks an instance's look-back waits on have started before it.
+// One-pass allocation of every instance: a block's chunk within its
+// instance comes from the instance's ticket, so the blocks an instance's
+// look-back waits on have started before it.
 template <int MODE>
 __global__ void __launch_bounds__(RB, 8) k3_alloc_b(cvg_realloc_batch B)
 {
@@ -1354,13 +1335,8 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
     if (fast) k3_results_b<true><<<B.total_blocks, RB, 0, s>>>(B);    // + finish per instance
     else k3_results_b<false><<<B.total_blocks, RB, 0, s>>>(B);
     if (adapt) {
-        if (B.one_pass) {
-            if (fast) k3_alloc_b<2><<<B.total_blocks, RB, 0, s>>>(B);
-            else k3_alloc_b<0><<<B.total_blocks, RB, 0, s>>>(B);
-        } else {
-            k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 0);  // + scan per instance
-            k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 0);
-        }
+        if (fast) k3_alloc_b<2><<<B.total_blocks, RB, 0, s>>>(B);
+        else k3_alloc_b<0><<<B.total_blocks, RB, 0, s>>>(B);
     }
     k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
@@ -1369,12 +1345,7 @@ cudaError_t cvg_launch_realloc_batch(const cvg_realloc_batch &B, int adapt, bool
 cudaError_t cvg_launch_set_nh_batch(const cvg_realloc_batch &B, const cvg_batch_sched &S,
                                     cudaStream_t s)
 {
-    if (B.one_pass) {
-        k3_alloc_b<1><<<B.total_blocks, RB, 0, s>>>(B);
-    } else {
-        k3_count_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
-        k3_apply_b<<<B.total_blocks, RB, 0, s>>>(B, 1);
-    }
+    k3_alloc_b<1><<<B.total_blocks, RB, 0, s>>>(B);
     k_tile_base<<<1, 1024, 0, s>>>(B, S);
     return cudaGetLastError();
 }

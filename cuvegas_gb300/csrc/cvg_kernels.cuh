@@ -87,7 +87,6 @@ struct cvg_realloc_batch {
     const unsigned *blk_inst;     // [total_blocks] instance of each block
     unsigned total_blocks;
     int n;
-    int one_pass;                 // 1: every instance has look-back words (k3_alloc)
 };
 struct cvg_refine_batch {
     const cvg_refine_args *R;     // [n]
