@@ -14,7 +14,7 @@ from oracle.ref_build import REF as REF_ROOT
 HERE = os.path.dirname(os.path.abspath(__file__))
 CFG = os.path.join(HERE, "golden", "cli", "config.cuh")
 SRC = os.path.join(HERE, "golden", "cli", "peaks.cu")
-REF = os.path.join(REF_ROOT, "src")     # the reference checkout, present only where it was surveyed
+REF = os.path.join(REF_ROOT, "src")     # the reference sources, present only on the machine that holds them
 
 
 def _cli(*args, timeout=600):
