@@ -55,6 +55,7 @@ struct inst_host {
     int *scale_exp;
     double *scale_ss;
     int *bin_exp;
+    double *exp_dq;         // [0] sum of d_h * q; the int after it: the next fill's exponent shift
     cvg_u32 *done;
     cvg_u64 *nh_sum, *bsums, *lb;
     cvg_u32 *lb_ctl;
@@ -127,6 +128,7 @@ void inst_layout(inst_host &h, int N, int max_it, char *base, size_t &off)
     place(h.scale_ss, 16, base, off);
     place(h.done, 16, base, off);
     place(h.bin_exp, sizeof(int) * (D * N + 1), base, off);
+    place(h.exp_dq, 16, base, off);
     place(h.theta, sizeof(double) * std::max(1, h.n_params), base, off);
     place(h.grad, sizeof(double) * std::max(1, h.n_params), base, off);
 }
@@ -421,6 +423,8 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         a.scale_ss = p.precision == CVG_PREC_FP32 ? h.scale_ss : nullptr;
         a.bin_exp = p.precision == CVG_PREC_FP32 ? h.bin_exp : nullptr;
         a.hist_state = nullptr;   // batched fills always keep fixed-point bin sums
+        a.exp_shift = p.precision == CVG_PREC_FP32 ? reinterpret_cast<const int *>(h.exp_dq + 1)
+                                                   : nullptr;
         a.max_tiles = h.max_tiles;
         a.seed = p.seed;
         a.instance = insts[i].instance;
@@ -457,6 +461,8 @@ cvg_status batch_init(cvg_batch_s *b, const cvg_instance *insts, const double *t
         r.max_it = p.max_it;
         r.fast_pow = p.precision == CVG_PREC_FP32 ? 1 : 0;
         r.hist_state = nullptr;
+        r.exp_dq = p.precision == CVG_PREC_FP32 ? h.exp_dq : nullptr;
+        r.exp_shift = p.precision == CVG_PREC_FP32 ? reinterpret_cast<int *>(h.exp_dq + 1) : nullptr;
         r.dim = D;
         r.adapt = (p.flags & CVG_FLAG_NO_ADAPT) ? 0 : 1;
         r.lb = h.lb;            // one-pass allocation; the words start at zero (arena)

@@ -60,6 +60,9 @@ struct cvg_fill_args {
     int *bin_exp;                 // FP32 form: [dim][N] binary exponent of each bin's expected
                                   // per-sample (f*jac)^2 (unscaled); [dim*N] = the scale
                                   // exponent k of the last fill (null for FP64)
+    const int *exp_shift;         // batched FP32 fills: bits added to every bin's exponent, the
+                                  // predicted rise of the per-sample (f*jac)^2 after the last
+                                  // reallocation (null: none)
     cvg_u64 max_tiles;            // capacity of tile_cube
     cvg_u64 seed;                 // Philox key
     cvg_u32 instance;             // Philox counter word 3, bits 8..31

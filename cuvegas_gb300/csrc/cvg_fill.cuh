@@ -336,10 +336,10 @@ template <bool FIX> CVG_D cvg_u32 cvg_hist_count(cvg_u32 w) { return FIX ? (w & 
 // Cleared count word of bin i: with fixed point it carries the bin's scale
 // exponent (unscaled exponent from the table minus 2k for the f*jac scaling).
 template <bool FIX>
-CVG_D cvg_u32 cvg_hist_word(const cvg_fill_args &a, int i, int kx)
+CVG_D cvg_u32 cvg_hist_word(const cvg_fill_args &a, int i, int kx, int shift)
 {
     if (!FIX) return 0u;
-    int e = a.bin_exp ? a.bin_exp[i] - 2 * kx : 0;
+    int e = a.bin_exp ? a.bin_exp[i] - 2 * kx + shift : 0;
     e = e < -100 ? -100 : (e > 100 ? 100 : e);
     return (cvg_u32)e << 24;
 }
@@ -533,9 +533,10 @@ CVG_D void cvg_fill_setup(const cvg_fill_args &a, const cvg_fill_smem<D, T, ESM,
     cx.kx = (sizeof(T) == 4 && a.scale_exp) ? *a.scale_exp : 0;
     cx.jac0 = cvg_scale_pow2((T)0, cx.kx);
     if (H) {
+        const int shift = (FIX && a.exp_shift) ? *a.exp_shift : 0;
         for (int i = tid; i < D * N; i += BS) {
             sm.hw[i] = (T)0;
-            sm.hc[i] = cvg_hist_word<FIX>(a, i, cx.kx);
+            sm.hc[i] = cvg_hist_word<FIX>(a, i, cx.kx, shift);
         }
         // the refinement turns this fill's bin sums (units 2^-2k) back into
         // unscaled exponents for the next fill's table

@@ -201,7 +201,11 @@ template <int R = RIPT>
 __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double wsum[4][RB / 32];
+    __shared__ float wdq[RB / 32];
     const cvg_u32 base = blk * (cvg_u32)(RB * R);
+    // batched runs: sum of d_h * q (2^-64) for the next fill's exponent shift
+    const bool xq = a.exp_dq != nullptr;
+    float sdq = 0.f;
     const float beta = (float)a.beta;
     const int kx = a.scale_exp ? *a.scale_exp : 0;   // work on JF*2^-k, JF2*2^-2k
     dfloat sm = {0.f, 0.f};
@@ -257,6 +261,7 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
             const float y = dh - kd, t = sd + y;
             kd = (t - sd) - y; sd = t;
         }
+        if (xq) sdq = fmaf(dh * 0x1p-32f, qq * 0x1p-32f, sdq);
         DH[c] = dh;
     }
     // warp reduction in FP32 (double-float for the estimate)
@@ -268,9 +273,11 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
         v += __shfl_down_sync(0xffffffffu, v, o);
         d += __shfl_down_sync(0xffffffffu, d, o);
         sq += __shfl_down_sync(0xffffffffu, sq, o);
+        if (xq) sdq += __shfl_down_sync(0xffffffffu, sdq, o);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
+        wdq[warp] = sdq;
         wsum[0][warp] = f2d_bits(d);
         wsum[1][warp] = f2d_bits(sm.h) + f2d_bits(sm.l);
         wsum[2][warp] = f2d_bits(v);
@@ -286,6 +293,11 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
         a.partials[4 * blk + 1] = t1;
         a.partials[4 * blk + 2] = t2;
         a.partials[4 * blk + 3] = t3;
+        if (xq) {
+            double t4 = 0.0;
+            for (int w = 0; w < RB / 32; ++w) t4 += f2d_bits(wdq[w]);
+            atomicAdd(a.exp_dq, t4);
+        }
     }
 }
 
@@ -321,6 +333,7 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
         const double sw = acc->sw, swr = acc->swr, swr2 = acc->swr2;
         const cvg_u64 used = acc->used, tot = acc->tot_nevals;
         const cvg_u32 rare_n = a.hist_state ? a.hist_state[1] : 0u;
+        const double dq = a.exp_dq ? *a.exp_dq : 0.0;
 
         double r = v[1], s = v[2];
         int knew = kx;
@@ -346,6 +359,22 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
                                 ldexp((double)rare_n, a.rare_shift) <= (double)S * (double)a.dim;
 
         if (a.fast_pow && a.scale_exp) *a.scale_exp = knew;
+        if (a.exp_dq && a.exp_shift) {
+            // batched FP32 form: the next fill samples hypercube c about
+            // n_eval d_h/sum(d_h) times, so its mean per-sample (f*jac)^2 is
+            // near sum(d_h q)/sum(d_h), against sum(JF2)/S in this fill (q =
+            // JF2/n of c, both in 2^-2k units); the exponent table (per-bin
+            // means of this fill) is raised by that ratio's whole bits
+            const double enew = ldexp(dq, 64) / v[0], eold = v[3] / (double)S;
+            int sh = 0;
+            if (enew > 0.0 && eold > 0.0 && isfinite(enew) && isfinite(eold)) {
+                int e = 0;
+                frexp(enew / eold, &e);
+                sh = e - 1 < 0 ? 0 : (e - 1 > 40 ? 40 : e - 1);
+            }
+            *a.exp_shift = sh;
+            *a.exp_dq = 0.0;
+        }
         if ((int)it < a.max_it) {
             a.stats[it] = r;
             a.stats[a.max_it + it] = s;

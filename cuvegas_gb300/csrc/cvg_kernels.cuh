@@ -62,6 +62,10 @@ struct cvg_realloc_args {
                             // CVG_KSTAT_TIMEOUT; 0 = the default (2^22)
     cvg_u32 lb_withhold;    // failure test only: 1 + the chunk whose look-back word is never
                             // published (its successors' waits then run out); 0 = none
+    double *exp_dq;         // batched FP32 form: sum over hypercubes of d_h * (JF2/n) 2^-2k,
+                            // 2^-64 (the results blocks add, the finish reads and clears), or null
+    int *exp_shift;         // batched FP32 form: the next fill's exponent shift (cvg_fill_args),
+                            // set by the finish; or null
 };
 
 struct cvg_refine_args {
