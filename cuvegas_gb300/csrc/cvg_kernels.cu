@@ -197,14 +197,14 @@ __global__ void __launch_bounds__(RB) k3_results(cvg_realloc_args a)
 // d_h = (q - m^2)^beta (the constant V^(2 beta) cancels in the allocation).
 // Sums are compensated in FP32 per thread, FP64 across warps and blocks;
 // k3_finish multiplies by V and V^2.
-template <int R = RIPT>
+template <int R = RIPT, bool XQ = false>
 __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, const unsigned blk)
 {
     __shared__ double wsum[4][RB / 32];
-    __shared__ float wdq[RB / 32];
+    __shared__ float wdq[XQ ? RB / 32 : 1];
     const cvg_u32 base = blk * (cvg_u32)(RB * R);
-    // batched runs: sum of d_h * q (2^-64) for the next fill's exponent shift
-    const bool xq = a.exp_dq != nullptr;
+    // XQ (batched runs): sum of d_h * q (2^-64) for the next fill's exponent shift
+    const bool xq = XQ && a.exp_dq != nullptr;
     float sdq = 0.f;
     const float beta = (float)a.beta;
     const int kx = a.scale_exp ? *a.scale_exp : 0;   // work on JF*2^-k, JF2*2^-2k
@@ -277,7 +277,7 @@ __device__ __forceinline__ void k3_results_f32_dev(const cvg_realloc_args &a, co
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
-        wdq[warp] = sdq;
+        if (xq) wdq[warp] = sdq;
         wsum[0][warp] = f2d_bits(d);
         wsum[1][warp] = f2d_bits(sm.h) + f2d_bits(sm.l);
         wsum[2][warp] = f2d_bits(v);
@@ -963,7 +963,7 @@ __global__ void __launch_bounds__(RB, 4) k3_results_b(cvg_realloc_batch B)
 {
     const int i = (int)B.blk_inst[blockIdx.x];
     const cvg_realloc_args &a = B.A[i];
-    if (FAST) k3_results_f32_dev(a, blockIdx.x - B.blk_base[i]);
+    if (FAST) k3_results_f32_dev<RIPT, true>(a, blockIdx.x - B.blk_base[i]);
     else k3_results_dev(a, blockIdx.x - B.blk_base[i]);
     const unsigned nb = B.blk_base[i + 1] - B.blk_base[i];
     if (last_block(&a.done[0], nb)) k3_finish_dev(a, nb);
