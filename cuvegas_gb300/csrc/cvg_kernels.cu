@@ -365,9 +365,10 @@ __device__ void k3_finish_dev(const cvg_realloc_args &a, unsigned nb)
             // near sum(d_h q)/sum(d_h), against sum(JF2)/S in this fill (q =
             // JF2/n of c, both in 2^-2k units); the exponent table (per-bin
             // means of this fill) is raised by that ratio's whole bits
+            // (without adaptation the allocation does not follow d_h: no shift)
             const double enew = ldexp(dq, 64) / v[0], eold = v[3] / (double)S;
             int sh = 0;
-            if (enew > 0.0 && eold > 0.0 && isfinite(enew) && isfinite(eold)) {
+            if (a.adapt && enew > 0.0 && eold > 0.0 && isfinite(enew) && isfinite(eold)) {
                 int e = 0;
                 frexp(enew / eold, &e);
                 sh = e - 1 < 0 ? 0 : (e - 1 > 40 ? 40 : e - 1);
